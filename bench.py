@@ -1,0 +1,438 @@
+"""Benchmark: DNS steps/s of the channel time step, one JSON line on stdout.
+
+Workload: the Re_tau = 550 channel, 384 x 257 x 384 modes (576 x 257 x 576
+dealiased physical points), seeded divergence-free perturbation; FP64 (the
+reference's arithmetic) is the headline, the mixed-precision variant (FP32
+transforms and products, FP64 solves) is measured beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fp64|mixed] [--workload channel_550|channel_180]
+
+N > 1 is launched by torchrun, one rank per GPU; every rank advances its own
+independent channel (the step does not shard across GPUs here: replicas),
+timed between barriers, max over ranks.  ``--impl reference`` times the CPU
+restatement of the reference algorithm (oracle/owt_port.cpp: dense per-mode
+LU, as src/solver.cpp does) on the host cores, rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "open-3d-wallturbulence_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "DNS steps/s at Re_tau=550 384x257x384: FP64 vs mixed (<=1e-6 rel RHS err)"
+DATA = ("synthetic: laminar Poiseuille + seeded divergence-free random perturbation "
+        "(Gaussian amplitudes, k^-2 spectrum, RMS 0.1 U_b, zero at walls), seed 0")
+
+
+def workload(name):
+    from owt.params import channel_550, channel_180
+    return {"channel_550": channel_550, "channel_180": channel_180}[name]()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled while the timed region runs
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 8:
+                self.rows.append(parts)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[4 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work per stage (fixed formulas; see the design doc for derivations)
+# ---------------------------------------------------------------------------
+def stage_work(p):
+    import math
+    NY, M, NXH, NZ2, NX2 = p.NY, p.NZ * p.NXH, p.NXH, p.NZ2, p.NX2
+    S = 16.0 * NY * M  # bytes per spectral field
+    # banded systems: v-system 5NY unknowns (kl 18, ku 15), omega_y-system 2NY (6, 6);
+    # per column and complex rhs: 2 * 2 * (2 kl + ku) flops (forward + backward)
+    fl_modes = M * (5 * NY * 4 * (2 * 18 + 15) + 2 * NY * 4 * (2 * 6 + 6) + 120 * NY)
+    fl_fft = lambda n: 5.0 * n * math.log2(n)
+    n_z = 9 * NXH * NY                 # 6 backward + 3 forward z lines
+    n_x = 4.5 * NZ2 * NY               # 3 packed backward + 1.5 packed forward x lines
+    fl_lamb = n_z * fl_fft(NZ2) + n_x * fl_fft(NX2) + 9.0 * NX2 * NZ2 * NY
+    fl_nl = M * NY * 60.0
+    unique = NXH * (p.NZ // 2 + 1)
+    factor_bytes = 8.0 * unique * (5 * NY * (2 * 18 + 15 + 1) + 2 * NY * (2 * 6 + 6 + 1))
+    return {
+        "modes": {"flops": fl_modes, "bytes": 22 * S + factor_bytes},
+        "lamb": {"flops": fl_lamb, "bytes": 9 * S},
+        "nonlinear": {"flops": fl_nl, "bytes": 5 * S},
+    }
+
+
+def measure_fp64_peak():
+    """cuBLAS DGEMM throughput (torch.matmul, float64) as the FP64 denominator."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    from owt.ic import seeded_velocity
+    from owt.solver import GpuSolver
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    p = workload(args.workload)
+    u, v, w = seeded_velocity(p, seed=0)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed_steps(solver, k):
+        st = torch.cuda.ExternalStream(solver.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(st)
+        solver.time_Integration(k)
+        e1.record(st)
+        solver.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    results = {}
+    precisions = [args.precision] + [q for q in ("fp64", "mixed") if q != args.precision]
+    solver = GpuSolver(p, precision=args.precision, device=local_rank)
+    solver.init_fields(u, v, w)
+    solver.use_graph(True)
+    clocks = None
+    for prec in precisions:
+        solver.set_precision(prec)
+        solver.init_fields(u, v, w)
+        solver.time_Integration(args.warmup)
+        solver.synchronize()
+        l0 = solver.launch_count
+        if prec == args.precision:
+            with ClockSampler(local_rank) as cs:
+                ms = timed_steps(solver, args.steps)
+            clocks = cs.summary()
+        else:
+            ms = timed_steps(solver, args.steps)
+        launches = solver.launch_count - l0
+        results[prec] = {"ms_per_step": ms / args.steps, "steps_per_s": 1e3 * args.steps / ms,
+                         "gpu_launches": launches}
+
+    # one-step RHS error of the mixed variant against FP64 (same state)
+    rhs_err = None
+    if rank == 0:
+        solver.set_precision("fp64")
+        solver.init_fields(u, v, w)
+        solver.time_Integration(1)
+        ref = {n: solver.get(n) for n in ("lmbx", "lmby", "lmbz", "Hv", "Hg", "vely", "vory")}
+        solver.set_precision("mixed")
+        solver.init_fields(u, v, w)
+        solver.time_Integration(1)
+        rhs_err = {n: float(np.linalg.norm(solver.get(n) - ref[n]) / max(np.linalg.norm(ref[n]), 1e-300))
+                   for n in ref}
+        del ref
+
+    # per-stage timing with CUDA events on the library stream (dominant kernel)
+    stage_ms = {}
+    if rank == 0:
+        solver.set_precision(args.precision)
+        solver.use_graph(False)
+        solver.init_fields(u, v, w)
+        st = torch.cuda.ExternalStream(solver.stream)
+        reps = max(3, min(10, args.steps))
+        for name, sid in (("modes", 0), ("lamb", 2), ("nonlinear", 3)):
+            solver.enqueue_stage(sid)
+            solver.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                solver.enqueue_stage(sid)
+            e1.record(st)
+            solver.synchronize()
+            stage_ms[name] = e0.elapsed_time(e1) / reps
+
+    # end to end through the C ABI with host buffers: every step uploads the
+    # full step input (12 history fields, 12 mean vectors, 6 friction values)
+    # from pinned memory and reads back the new v, omega_y and friction.
+    e2e = None
+    if True:
+        solver.use_graph(True)
+        solver.set_precision(args.precision)
+        solver.init_fields(u, v, w)
+        solver.time_Integration(1)
+        hist = ["vely_0", "vely_1", "vely_2", "vory_0", "vory_1", "vory_2",
+                "Hv_0", "Hv_1", "Hv_2", "Hg_0", "Hg_1", "Hg_2"]
+        means = ["lmbx_mean_0", "lmbx_mean_1", "lmbx_mean_2", "lmbz_mean_0", "lmbz_mean_1", "lmbz_mean_2",
+                 "velx_mean_0", "velx_mean_1", "velx_mean_2", "velz_mean_0", "velz_mean_1", "velz_mean_2"]
+
+        def pinned(shape):
+            return torch.empty(tuple(shape) + (2,), dtype=torch.float64, pin_memory=True).numpy().view(
+                np.complex128).reshape(shape)
+
+        host_in = {n: pinned(p.spectral_shape) for n in hist}
+        for n in hist:
+            solver.get(n, out=host_in[n])
+        host_mean = {n: solver.get_cvec(n) for n in means}
+        fric = solver.friction()
+        out_v, out_g = pinned(p.spectral_shape), pinned(p.spectral_shape)
+        k_e2e = max(2, min(args.steps, 5))
+        bi = len(hist) * host_in[hist[0]].nbytes + len(means) * p.NY * 16 + 48
+        bo = out_v.nbytes + out_g.nbytes + 48
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            for n in hist:
+                solver.set(n, host_in[n])
+            for n in means:
+                solver.set_cvec(n, host_mean[n])
+            solver.set_friction(fric)
+            solver.time_Integration(1)
+            solver.get("vely", out=out_v)
+            solver.get("vory", out=out_g)
+            solver.friction()
+        barrier()
+        dt_e2e = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([dt_e2e], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt_e2e = float(t.item())
+        e2e = {"value": world * k_e2e / dt_e2e, "unit": "steps/s", "h2d_bytes_per_step": int(bi),
+               "d2h_bytes_per_step": int(bo)}
+    solver.close()
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return None
+
+    peaks, peak_kind = load_peaks()
+    fp64_peak = measure_fp64_peak()
+    work = stage_work(p)
+    dom = max(("modes", "lamb", "nonlinear"), key=lambda n: stage_ms.get(n, 0.0))
+    t_dom = stage_ms[dom] * 1e-3
+    fl_dom = work[dom]["flops"]
+    if args.precision == "mixed" and dom == "lamb":
+        roof = {"bound": "hbm", "achieved": work[dom]["bytes"] / t_dom / 1e9, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s"}
+    else:
+        roof = {"bound": "fp64", "achieved": fl_dom / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["kernel"] = dom
+    roof["traffic"] = None
+    roof["peak_source"] = ("cuBLAS DGEMM (torch.matmul float64, 4096^3) measured in this run"
+                           if roof["bound"] == "fp64" else f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})")
+    roof["stage_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
+    roof["stage_hbm_gbs"] = {k: round(work[k]["bytes"] / (stage_ms[k] * 1e-3) / 1e9, 1) for k in stage_ms}
+    roof["stage_fp64_tflops"] = {k: round(work[k]["flops"] / (stage_ms[k] * 1e-3) / 1e12, 3) for k in stage_ms}
+
+    head = results[args.precision]
+    value = world * head["steps_per_s"]
+    line = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(head["ms_per_step"], 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": DATA,
+        "config": {
+            "workload": f"{args.workload}_{p.NX}x{p.NY}x{p.NZ}",
+            "modes": [p.NX, p.NY, p.NZ], "physical": [p.NX2, p.NY, p.NZ2],
+            "dt": p.dt, "nu": p.nu, "precision": args.precision, "cuda_graph": True,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (the step streams ~40 GB of state and factors)",
+            "grid_point_updates_per_s": round(value * p.NX2 * p.NZ2 * p.NY, 1),
+        },
+        "variants": {q: {"steps_per_s": round(world * r["steps_per_s"], 4), "ms_per_step": round(r["ms_per_step"], 4)}
+                     for q, r in results.items()},
+        "roofline": roof,
+        "gpu_launches": head["gpu_launches"],
+        "clocks": clocks,
+        "e2e": e2e,
+    }
+    if "fp64" in results and "mixed" in results:
+        line["variants"]["mixed"]["speedup_vs_fp64"] = round(results["fp64"]["ms_per_step"] /
+                                                             results["mixed"]["ms_per_step"], 3)
+        line["variants"]["mixed"]["rhs_rel_l2_err_vs_fp64"] = {k: float("%.3e" % x) for k, x in rhs_err.items()}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(p, args, quick=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference algorithm (oracle restatement) on the host cores
+# ---------------------------------------------------------------------------
+def build_port():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+
+
+def cpu_sample(p, mode_stride, fields):
+    """Seconds of one full step extrapolated from a bounded sample: the mode
+    loop over every mode_stride-th mode (the dense per-mode LU solves) and
+    `fields` inverse (+ fields/2 forward) transforms, scaled up to all modes
+    and 9 transforms; the dense DY mat-vecs are included at their share."""
+    from oracle import PortOracle
+    o = PortOracle()
+    o.init(p.dt, p.dkx, p.dkz, p.NX, p.NY, p.NZ, p.alpha_mesh, p.nu)
+    M = p.NZ * p.NXH
+    n_sampled = len(range(0, M, mode_stride))
+    t_modes = o.lib.port_time_modes(mode_stride, 1) * (M / n_sampled)
+    t_xf = o.lib.port_time_transforms(fields) * (9.0 / (fields + fields // 2))
+    return o, t_modes + t_xf
+
+
+def cpu_baseline(p, args, quick=False):
+    build_port()
+    from oracle import PortOracle
+    threads = PortOracle().set_threads(0)
+    stride = max(1, (p.NZ * p.NXH) // (256 if quick else 512))
+    _, t = cpu_sample(p, stride, 2)
+    return {"value": round(1.0 / t, 6), "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"mode loop over every {stride}th mode + 2 inverse/1 forward transforms, "
+                      f"scaled to one full step ({t:.1f} s/step extrapolated)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    p = workload(args.workload)
+    build_port()
+    from oracle import PortOracle
+    threads = PortOracle().set_threads(0)
+    stride = max(1, (p.NZ * p.NXH) // 256)
+    for _ in range(args.warmup):
+        cpu_sample(p, stride * 4, 1)
+    ts = []
+    for _ in range(args.steps):
+        _, t = cpu_sample(p, stride, 2)
+        ts.append(t)
+    t = statistics.mean(ts)
+    value = 1.0 / t
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": f"{args.workload}_{p.NX}x{p.NY}x{p.NZ}", "precision": "fp64",
+                   "implementation": "CPU restatement of the reference algorithm (dense per-mode LU, "
+                                     "dense DY mat-vecs, FFT-based dealiased transforms), OpenMP"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: mode loop over every {stride}th mode + 3 transforms, "
+                                   f"extrapolated to one full step"},
+        "e2e": {"value": round(value, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--workload", choices=["channel_550", "channel_180"], default="channel_550")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local_rank)
+    if line is not None and rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

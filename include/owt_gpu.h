@@ -1,0 +1,178 @@
+/*
+ * owt_gpu.h -- C ABI of the GB300 channel-DNS time step.
+ *
+ * Drop-in boundary for the reference solver's per-step entry points.  The
+ * reference keeps its state in C++ inline globals (src/setup.hpp:22-79) and
+ * exposes free functions (src/setup.hpp:84-114) called from its driver loop
+ * (src/main.cpp:63-87).  This library keeps the same state on one GPU behind an
+ * opaque handle; every function below names the reference routine or global it
+ * replaces.  Only plain pointers, sizes and integers cross this interface.
+ *
+ * Conventions
+ *  - Host arrays are in the reference Field layout [z][x][y] (src/linalg.hpp:
+ *    695-745): NZ * (NX/2) * NY complex values, complex128 stored as
+ *    interleaved (re, im) doubles.  Mean-mode vectors are NY complex128.
+ *  - Every call returns an int status: OWT_OK (0) on success.  On failure
+ *    owt_last_error() returns a message (the reference throws
+ *    std::runtime_error in the same places, src/linalg.hpp:519,643).
+ *  - The caller owns host buffers; the library owns device memory and its
+ *    CUDA stream.  Calls on one handle must not overlap (the reference is
+ *    single-threaded per rank); separate handles are independent.
+ *  - Get/set calls are synchronous: when they return, the host buffer has
+ *    been read or written.
+ */
+#ifndef OWT_GPU_H
+#define OWT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define OWT_OK 0
+#define OWT_ERR_INVALID 1   /* bad argument or size (src/parallel.cpp:40-44 analogue) */
+#define OWT_ERR_CUDA 2      /* CUDA runtime error */
+#define OWT_ERR_NUMERIC 3   /* singular factorization or non-finite state */
+#define OWT_ERR_STATE 4     /* call made in the wrong order */
+#define OWT_ERR_NOMEM 5     /* device allocation failed */
+
+/* arithmetic of the x/z transforms and physical-space products */
+#define OWT_PREC_FP64 0     /* everything in FP64, as the reference */
+#define OWT_PREC_MIXED 1    /* transforms + products in FP32; solves, factors,
+                               mean mode and friction stay FP64 */
+
+typedef struct owt_handle owt_handle;
+
+/* Case parameters: the TOML keys read by load_params (src/IO.cpp:14-25).
+ * PX, PZ, NT and save_interval concern the driver, not the step. */
+typedef struct owt_params {
+  double dt;          /* time step */
+  double dkx, dkz;    /* fundamental wavenumbers: Lx = 2 pi/dkx, Lz = 2 pi/dkz */
+  double alpha_mesh;  /* tanh stretching factor, y = tanh(alpha s)/tanh(alpha) */
+  double nu;          /* kinematic viscosity */
+  int64_t NX, NY, NZ; /* modes: NX/2 kx, NZ kz, NY wall-normal points */
+  int32_t precision;  /* OWT_PREC_FP64 or OWT_PREC_MIXED */
+  int32_t device;     /* CUDA device ordinal */
+} owt_params;
+
+/* Spectral fields, the reference globals of the same names
+ * (src/setup.hpp:58-67).  On the device vely/vory/Hv/Hg share storage with
+ * vely_0/vory_0/Hv_0/Hg_0: the reference makes them equal at the end of every
+ * step (src/solver.cpp:612-626) and after init_fields (:383-397). */
+enum owt_field {
+  OWT_VELX = 0, OWT_VELY, OWT_VELZ,
+  OWT_VORX, OWT_VORY, OWT_VORZ,
+  OWT_LMBX, OWT_LMBY, OWT_LMBZ,
+  OWT_HV, OWT_HG,
+  OWT_VELY_0, OWT_VELY_1, OWT_VELY_2,
+  OWT_VORY_0, OWT_VORY_1, OWT_VORY_2,
+  OWT_HV_0, OWT_HV_1, OWT_HV_2,
+  OWT_HG_0, OWT_HG_1, OWT_HG_2,
+  OWT_NUM_FIELDS
+};
+
+/* Mean-mode history vectors (src/setup.hpp:68-71). */
+enum owt_mean {
+  OWT_LMBX_MEAN_0 = 0, OWT_LMBX_MEAN_1, OWT_LMBX_MEAN_2,
+  OWT_LMBZ_MEAN_0, OWT_LMBZ_MEAN_1, OWT_LMBZ_MEAN_2,
+  OWT_VELX_MEAN_0, OWT_VELX_MEAN_1, OWT_VELX_MEAN_2,
+  OWT_VELZ_MEAN_0, OWT_VELZ_MEAN_1, OWT_VELZ_MEAN_2,
+  OWT_NUM_MEANS
+};
+
+/* Individual reference routines, run on the handle's state (owt_call). */
+enum owt_routine {
+  OWT_CALL_GET_VOR_FROM_VEL = 0, /* src/solver.cpp:218-238 */
+  OWT_CALL_LAMB_VEC,             /* src/solver.cpp:262-304 (incl. mean-Lamb history shift) */
+  OWT_CALL_NONLINEAR_SOURCE,     /* src/solver.cpp:240-260 */
+  OWT_CALL_SOLVE_FRICTION_FORCE, /* src/solver.cpp:306-327 */
+  OWT_CALL_TIME_INTEGRATION      /* src/solver.cpp:541-627 */
+};
+
+/* Create a handle: replaces allocate_var + init_mat + init_fft
+ * (src/solver.cpp:15-216, src/FFT.cpp:11-34).  Builds the grid, metric,
+ * compact-FD operators and the per-mode banded factorizations on the device. */
+int owt_create(const owt_params *params, owt_handle **out);
+
+/* Free everything (cleanup_fft, src/FFT.cpp:36-47, and the field storage). */
+int owt_destroy(owt_handle *h);
+
+/* Message of the last failed call on h; h == NULL gives the calling thread's
+ * last owt_create failure. Never NULL. */
+const char *owt_last_error(const owt_handle *h);
+
+/* init_fields (src/solver.cpp:329-426) with a caller-given velocity field in
+ * place of the reference's built-in laminar + TS-wave one: vorticity from
+ * velocity, Lamb vector, sources, history levels all equal, friction, mean
+ * histories.  velx/vely/velz: [z][x][y] complex128. */
+int owt_init_fields(owt_handle *h, const double *velx, const double *vely, const double *velz);
+
+/* time_Integration (src/solver.cpp:541-627), nsteps times. Asynchronous on
+ * the handle's stream; errors found on the device surface at the next
+ * synchronizing call. */
+int owt_time_integration(owt_handle *h, int64_t nsteps);
+
+/* Run one reference routine on the current state (enum owt_routine). */
+int owt_call(owt_handle *h, int routine);
+
+/* Wait for all work on the handle; reports device-side numeric failures. */
+int owt_synchronize(owt_handle *h);
+
+/* Copy a spectral field (enum owt_field) between host [z][x][y] complex128
+ * and the device. */
+int owt_get_field(owt_handle *h, int field, double *host);
+int owt_set_field(owt_handle *h, int field, const double *host);
+
+/* Mean-mode histories (enum owt_mean): NY complex128. */
+int owt_get_mean(owt_handle *h, int which, double *host);
+int owt_set_mean(owt_handle *h, int which, const double *host);
+
+/* Friction-force histories (src/setup.hpp:77-79):
+ * out[0..2] = fx_fric_0..2, out[3..5] = fz_fric_0..2. */
+int owt_get_friction(owt_handle *h, double *out6);
+int owt_set_friction(owt_handle *h, const double *in6);
+
+/* Select the transform precision (OWT_PREC_FP64 / OWT_PREC_MIXED). */
+int owt_set_precision(owt_handle *h, int precision);
+
+/* Capture one step in a CUDA graph and replay it in owt_time_integration
+ * (on = 1), or launch kernel by kernel (on = 0, the default). */
+int owt_use_graph(owt_handle *h, int on);
+
+/* Step counter since owt_init_fields (id_step in src/setup.hpp:34). */
+int owt_get_step(const owt_handle *h, int64_t *step);
+
+/* The handle's CUDA stream (a cudaStream_t), for ordering external work. */
+int owt_get_stream(const owt_handle *h, void **stream);
+
+/* Kernel launches issued by the library since the handle was created. */
+int owt_get_launch_count(const owt_handle *h, int64_t *count);
+
+/* Wall-normal grid y (src/solver.cpp:76) and DYn applied along y to every mode
+ * of a field: out = DYn * in for n = 1 or 2 (src/solver.cpp:182,193, applied as
+ * in src/linalg.hpp:434-453).  Arrays in the [z][x][y] layout. */
+int owt_get_grid(const owt_handle *h, double *y);
+int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
+
+/* Measurement aid, no counterpart in the reference: enqueue one stage of the
+ * step on the handle's stream without advancing the step counter, so a caller
+ * can time it with CUDA events on that stream.  The stage overwrites the
+ * state it would produce in a step (use a handle whose state is disposable).
+ *   0: mode kernel (RHS assembly, both implicit solves, solve_horizontal)
+ *   1: mean mode (solve_mean + friction)
+ *   2: transforms + products (Lamb vector, three kernels)
+ *   3: nonlinear source */
+#define OWT_STAGE_MODES 0
+#define OWT_STAGE_MEAN 1
+#define OWT_STAGE_LAMB 2
+#define OWT_STAGE_NONLINEAR 3
+int owt_enqueue_stage(owt_handle *h, int stage);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OWT_GPU_H */

@@ -1,0 +1,753 @@
+// C ABI of the GPU time step (declared in include/owt_gpu.h).
+//
+// One handle = one channel on one GPU: parameters, device-resident state,
+// per-mode band factorizations, scratch, and a CUDA stream.  A step is seven
+// launches: mode kernel, counter advance, mean mode, three transform kernels,
+// nonlinear source; it can be captured once as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "owt_gpu.h"
+#include "setup_host.h"
+#include "solve_kernels.h"
+
+using namespace owt;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct OwtError : std::runtime_error {
+  int code;
+  OwtError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+T *dalloc(size_t n, std::vector<void *> &owned) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw OwtError(OWT_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) +
+                                      " bytes failed: " + cudaGetErrorString(e));
+  }
+  owned.push_back(p);
+  return static_cast<T *>(p);
+}
+
+template <typename T>
+T *upload(const std::vector<T> &v, std::vector<void *> &owned, cudaStream_t st) {
+  T *d = dalloc<T>(v.size(), owned);
+  ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+  return d;
+}
+
+struct BandDev {
+  double *ab = nullptr;
+  uint8_t *piv = nullptr;
+  int n = 0, kl = 0, ku = 0;
+};
+
+}  // namespace
+
+struct owt_handle {
+  std::string err;
+  owt_params p{};
+  int NX = 0, NY = 0, NZ = 0, NXH = 0, NZH = 0, NX2 = 0, NZ2 = 0, M = 0, Uq = 0;
+  int precision = 0;
+  cudaStream_t st = nullptr;
+  std::vector<void *> owned;
+  int64_t steps = 0;
+  int64_t launches = 0;
+  bool initialized = false;
+  bool use_graph = false;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  bool q_dirty[3] = {false, false, false};
+  Grid grid;
+  double Ly = 0, inv_cg0 = 0;
+  size_t fs = 0;  // complex values per spectral field
+  // device constants
+  double *kx = nullptr, *kz = nullptr, *c11 = nullptr, *c21 = nullptr, *c22 = nullptr, *inv_cg = nullptr;
+  // state
+  double2 *v_ring = nullptr, *g_ring = nullptr, *hv_ring = nullptr, *hg_ring = nullptr, *q_ring = nullptr;
+  double2 *u = nullptr, *w = nullptr, *ox = nullptr, *oz = nullptr, *lx = nullptr, *ly = nullptr, *lz = nullptr;
+  double2 *U_ring = nullptr, *W_ring = nullptr, *lxm_ring = nullptr, *lzm_ring = nullptr;
+  double *fx_ring = nullptr, *fz_ring = nullptr;
+  long long *d_step = nullptr;
+  int *d_err = nullptr;
+  // factors and tables
+  BandDev bv, bg, b1, b2;
+  int *rhs_node_v = nullptr, *rb_col = nullptr, *b1_col = nullptr, *b2_col = nullptr;
+  double *rb_val = nullptr, *b1_val = nullptr, *b2_val = nullptr;
+  // scratch
+  double2 *sg = nullptr, *dg = nullptr, *yv = nullptr, *yg = nullptr;
+  double2 *mean_scratch = nullptr, *mean_dy1 = nullptr;
+  double2 *bf = nullptr, *yscr = nullptr, *tmpA = nullptr, *tmpB = nullptr, *tmpC = nullptr, *stage = nullptr;
+  void *zbuf = nullptr, *lbuf = nullptr;
+  void *twx[2] = {nullptr, nullptr}, *twz[2] = {nullptr, nullptr};
+  FftPlan px{}, pz{};
+
+  int head() const { return (int)((2 * (steps % 3)) % 3); }
+  int slot(int level) const { return (head() + level) % 3; }
+  double2 *ring_level(double2 *ring, int level) const { return ring + (size_t)slot(level) * fs; }
+
+  ~owt_handle() {
+    if (st) cudaStreamSynchronize(st);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void *q : owned) cudaFree(q);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  void check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+  }
+
+  // ---- setup -----------------------------------------------------------------
+  void setup(const owt_params &prm) {
+    p = prm;
+    NX = (int)p.NX; NY = (int)p.NY; NZ = (int)p.NZ;
+    if (p.NX < 4 || p.NZ < 4 || p.NX % 2 || p.NZ % 2)
+      throw OwtError(OWT_ERR_INVALID, "NX and NZ must be even and at least 4");
+    if (p.NY < 7) throw OwtError(OWT_ERR_INVALID, "N must be at least 7 for 3rd derivative scheme");
+    if (!(p.dt > 0) || !(p.nu > 0) || !(p.dkx > 0) || !(p.dkz > 0) || !(p.alpha_mesh > 0))
+      throw OwtError(OWT_ERR_INVALID, "dt, nu, dkx, dkz and alpha_mesh must be positive");
+    if (p.precision != OWT_PREC_FP64 && p.precision != OWT_PREC_MIXED)
+      throw OwtError(OWT_ERR_INVALID, "precision must be OWT_PREC_FP64 or OWT_PREC_MIXED");
+    NXH = NX / 2; NZH = NZ / 2; NX2 = NX / 2 * 3; NZ2 = NZ / 2 * 3;
+    M = NZ * NXH;
+    Uq = NXH * (NZH + 1);
+    fs = (size_t)NY * M;
+    precision = p.precision;
+    std::vector<int> rx, rz;
+    if (!fft_radices(NX2, rx) || !fft_radices(NZ2, rz))
+      throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must be of the form 2^a 3^b");
+    px.L = NX2; px.nst = (int)rx.size();
+    for (size_t q = 0; q < rx.size(); ++q) px.R[q] = rx[q];
+    pz.L = NZ2; pz.nst = (int)rz.size();
+    for (size_t q = 0; q < rz.size(); ++q) pz.R[q] = rz[q];
+    ck(cudaSetDevice(p.device), "cudaSetDevice");
+    ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+
+    // grid, metric, stencils, band templates (host, FP64)
+    grid = make_grid(NY, p.alpha_mesh);
+    Ly = grid.y[NY - 1] - grid.y[0];
+    Stencils sten = make_stencils(NY, grid.ds);
+    BandTemplate tv = build_v_system(grid, sten, p.nu);
+    BandTemplate tg = build_g_system(grid, sten, p.nu);
+    BandTemplate t1 = build_plain_band(sten, 0);
+    BandTemplate t2 = build_plain_band(sten, 1);
+    for (const BandTemplate *t : {&tv, &tg, &t1, &t2})
+      if (!band_supported(t->kl, t->ku))
+        throw OwtError(OWT_ERR_INVALID, "unsupported band width " + std::to_string(t->kl) + "/" + std::to_string(t->ku));
+
+    // wavenumbers exactly as allocate_var (src/solver.cpp:25-37, one rank)
+    std::vector<double> hkx(NXH), hkz(NZ);
+    for (int i = 0; i < NXH; ++i) hkx[i] = (double)i * p.dkx;
+    for (int k = 0; k < NZ; ++k) {
+      double t = (double)k;
+      if (t >= (double)NZH) t -= (double)NZ;
+      hkz[k] = t * p.dkz;
+    }
+    // per unique mode (|kz| index, kx index): a, b of Av and 1/cg of Ag
+    const double g0 = 11.0 / 6.0, dt = p.dt, nu = p.nu;
+    std::vector<double> sa(Uq), sb(Uq), icg(Uq);
+    for (int kabs = 0; kabs <= NZH; ++kabs)
+      for (int i = 0; i < NXH; ++i) {
+        const double kxv = hkx[i], kzv = hkz[kabs == NZH ? NZH : kabs];
+        const double k2 = std::pow(kxv, 2) + std::pow(kzv, 2), k4 = std::pow(k2, 2);
+        const int uq = kabs * NXH + i;
+        sa[uq] = g0 / dt + 2 * nu * k2;
+        sb[uq] = nu * k4 + g0 * k2 / dt;
+        icg[uq] = 1.0 / (nu * k2 + g0 / dt);
+      }
+    inv_cg0 = icg[0];
+
+    kx = upload(hkx, owned, st);
+    kz = upload(hkz, owned, st);
+    c11 = upload(grid.c11, owned, st);
+    c21 = upload(grid.c21, owned, st);
+    c22 = upload(grid.c22, owned, st);
+    inv_cg = upload(icg, owned, st);
+    d_step = dalloc<long long>(1, owned);
+    d_err = dalloc<int>(1, owned);
+    ck(cudaMemsetAsync(d_step, 0, sizeof(long long), st), "memset");
+    ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "memset");
+
+    // band factorizations
+    double *d_sa = upload(sa, owned, st), *d_sb = upload(sb, owned, st), *d_icg = inv_cg;
+    auto factor = [&](BandDev &bd, const BandTemplate &t, int U, const double *s1, const double *s2) {
+      bd.n = t.n; bd.kl = t.kl; bd.ku = t.ku;
+      const size_t nb = 2 * (size_t)t.kl + t.ku + 1;
+      bd.ab = dalloc<double>(nb * t.n * (size_t)U, owned);
+      bd.piv = dalloc<uint8_t>((size_t)t.n * U, owned);
+      std::vector<void *> tmp;
+      double *d0 = upload(t.t0, tmp, st), *d1 = upload(t.t1, tmp, st), *d2 = upload(t.t2, tmp, st);
+      launch_band_factor(t.kl, t.ku, bd.ab, bd.piv, t.n, U, d0, d1, d2, s1, s2, d_err, st);
+      ++launches;
+      check_launch("band factorization");
+      ck(cudaStreamSynchronize(st), "band factorization");
+      for (void *q : tmp) cudaFree(q);
+    };
+    factor(bv, tv, Uq, d_sa, d_sb);
+    factor(bg, tg, Uq, d_icg, nullptr);
+    factor(b1, t1, 1, nullptr, nullptr);
+    factor(b2, t2, 1, nullptr, nullptr);
+    int herr = 0;
+    ck(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost), "factor status");
+    if (herr) throw OwtError(OWT_ERR_NUMERIC, "LU factorization failed. Matrix A may be singular.");
+    rhs_node_v = upload(tv.rhs_node, owned, st);
+    rb_col = upload(tg.rb_col, owned, st);
+    rb_val = upload(tg.rb_val, owned, st);
+    // B1 / B2 rows as (col, val) x 5
+    auto brows = [&](int which, int *&dcol, double *&dval) {
+      std::vector<int> cols((size_t)NY * 5, 0);
+      std::vector<double> vals((size_t)NY * 5, 0.0);
+      for (int j = 0; j < NY; ++j) {
+        int e = 0;
+        for (int c = 0; c < NY; ++c) {
+          const double b = sten.b(which, j, c);
+          if (b != 0.0) {
+            if (e >= 5) throw std::logic_error("stencil row wider than 5");
+            cols[(size_t)j * 5 + e] = c;
+            vals[(size_t)j * 5 + e] = b;
+            ++e;
+          }
+        }
+      }
+      dcol = upload(cols, owned, st);
+      dval = upload(vals, owned, st);
+    };
+    brows(0, b1_col, b1_val);
+    brows(1, b2_col, b2_val);
+
+    // state and scratch
+    v_ring = dalloc<double2>(3 * fs, owned);
+    g_ring = dalloc<double2>(3 * fs, owned);
+    hv_ring = dalloc<double2>(3 * fs, owned);
+    hg_ring = dalloc<double2>(3 * fs, owned);
+    q_ring = dalloc<double2>(3 * fs, owned);
+    for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
+      *f = dalloc<double2>(fs, owned);
+    yv = dalloc<double2>((size_t)bv.n * M, owned);
+    yg = dalloc<double2>((size_t)bg.n * M, owned);
+    U_ring = dalloc<double2>(3 * (size_t)NY, owned);
+    W_ring = dalloc<double2>(3 * (size_t)NY, owned);
+    lxm_ring = dalloc<double2>(3 * (size_t)NY, owned);
+    lzm_ring = dalloc<double2>(3 * (size_t)NY, owned);
+    fx_ring = dalloc<double>(3, owned);
+    fz_ring = dalloc<double>(3, owned);
+    mean_scratch = dalloc<double2>(2 * (size_t)NY + 2 * (size_t)bg.n, owned);
+    mean_dy1 = dalloc<double2>(2 * (size_t)NY, owned);
+    XformDims xd{NY, NZ, NXH, NZH, NX2, NZ2};
+    ck(lamb_prepare(xd), "transform kernel attributes");
+    zbuf = dalloc<unsigned char>(lamb_zbuf_bytes(xd, 0), owned);
+    lbuf = dalloc<unsigned char>(lamb_lbuf_bytes(xd, 0), owned);
+    for (int prec = 0; prec < 2; ++prec) {
+      for (int axis = 0; axis < 2; ++axis) {
+        const int L = axis == 0 ? NX2 : NZ2;
+        std::vector<double> t = twiddles(L);
+        void *d;
+        if (prec == 0) {
+          d = upload(t, owned, st);
+        } else {
+          std::vector<float> tf(t.begin(), t.end());
+          d = upload(tf, owned, st);
+        }
+        (axis == 0 ? twx : twz)[prec] = d;
+      }
+    }
+    ck(cudaMemsetAsync(v_ring, 0, 3 * fs * sizeof(double2), st), "memset");
+    ck(cudaMemsetAsync(g_ring, 0, 3 * fs * sizeof(double2), st), "memset");
+    ck(cudaStreamSynchronize(st), "setup");
+  }
+
+  // ---- kernel sequences --------------------------------------------------------
+  void dapply(int order, const double2 *in, double2 *out) {
+    DApplyArgs a{};
+    a.NY = NY; a.M = M; a.in = in; a.out = out;
+    const BandDev &b = order == 1 ? b1 : b2;
+    a.ab = b.ab; a.piv = b.piv;
+    a.b_col = order == 1 ? b1_col : b2_col;
+    a.b_val = order == 1 ? b1_val : b2_val;
+    a.bf = bf; a.yscr = yscr;
+    launch_dapply(a, st);
+    ++launches;
+  }
+  XformArgs xform_args() {
+    XformArgs a{};
+    a.d = XformDims{NY, NZ, NXH, NZH, NX2, NZ2};
+    a.in[0] = u; a.in[1] = v_ring; a.in[2] = w; a.in[3] = ox; a.in[4] = g_ring; a.in[5] = oz;
+    a.ring_mask = (1 << 1) | (1 << 4);
+    a.fs = fs;
+    a.step = d_step;
+    a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
+    a.zbuf = zbuf; a.lbuf = lbuf;
+    a.px = px; a.pz = pz;
+    a.twx = twx[precision]; a.twz = twz[precision];
+    a.inv_nx2 = 1.0 / (double)NX2; a.inv_nz2 = 1.0 / (double)NZ2;
+    return a;
+  }
+  NLArgs nl_args(bool record_mean) {
+    NLArgs a{};
+    a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.M = M;
+    a.kx = kx; a.kz = kz; a.c11 = c11;
+    a.lx = lx; a.ly = ly; a.lz = lz;
+    a.hv_ring = hv_ring; a.hg_ring = hg_ring;
+    a.ab1 = b1.ab; a.piv1 = b1.piv; a.b1_col = b1_col; a.b1_val = b1_val;
+    a.bf = bf; a.yscr = yscr;
+    a.lx_mean = record_mean ? lxm_ring : nullptr;
+    a.lz_mean = record_mean ? lzm_ring : nullptr;
+    a.step = d_step;
+    return a;
+  }
+  // One time step.  Every argument is a fixed device pointer; which ring slot
+  // is which history level is read from the device step counter, so the same
+  // launch sequence (or its CUDA graph) serves every step.
+  void enqueue_step() {
+    stage_modes();
+    launch_advance(d_step, st);
+    stage_mean();
+    launch_lamb(xform_args(), precision, st);
+    launch_nl(nl_args(true), st);
+    launches += 7;
+  }
+  void stage_modes() {
+    ModeArgs a{};
+    a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.U = Uq;
+    a.inv_dt = 1.0 / p.dt; a.nu = p.nu;
+    a.kx = kx; a.kz = kz; a.c11 = c11; a.c21 = c21; a.c22 = c22;
+    a.v_ring = v_ring; a.g_ring = g_ring; a.hv_ring = hv_ring; a.hg_ring = hg_ring; a.q_ring = q_ring;
+    a.u_out = u; a.w_out = w; a.ox_out = ox; a.oz_out = oz;
+    a.ab_v = bv.ab; a.piv_v = bv.piv; a.n_v = bv.n;
+    a.ab_g = bg.ab; a.piv_g = bg.piv; a.n_g = bg.n;
+    a.rhs_node_v = rhs_node_v; a.rb_col = rb_col; a.rb_val = rb_val; a.inv_cg = inv_cg;
+    a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg;
+    a.step = d_step;
+    launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, st);
+  }
+  void stage_mean() {
+    MeanArgs ma{};
+    ma.NY = NY; ma.M = M; ma.U = Uq; ma.n_g = bg.n;
+    ma.inv_dt = 1.0 / p.dt; ma.nu = p.nu; ma.Ly = Ly; ma.inv_cg0 = inv_cg0;
+    ma.c11 = c11; ma.c21 = c21; ma.c22 = c22;
+    ma.ab_g = bg.ab; ma.piv_g = bg.piv; ma.rb_col = rb_col; ma.rb_val = rb_val;
+    ma.U_ring = U_ring; ma.W_ring = W_ring; ma.lx_ring = lxm_ring; ma.lz_ring = lzm_ring;
+    ma.fx_ring = fx_ring; ma.fz_ring = fz_ring;
+    ma.u_field = u; ma.w_field = w; ma.ox_field = ox; ma.oz_field = oz;
+    ma.scratch = mean_scratch; ma.dy1 = mean_dy1; ma.step = d_step; ma.err = d_err;
+    launch_mean(ma, st);
+  }
+
+  void run_steps(int64_t n) {
+    recompute_dirty_q();
+    if (use_graph) {
+      if (!gexec) {
+        ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const int64_t before = launches;
+        enqueue_step();
+        per_step_launches = launches - before;
+        launches = before;
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        ck(e, "end capture");
+        ck(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+      }
+      for (int64_t s = 0; s < n; ++s) {
+        ck(cudaGraphLaunch(gexec, st), "graph launch");
+        launches += per_step_launches;
+        ++steps;
+      }
+    } else {
+      for (int64_t s = 0; s < n; ++s) {
+        enqueue_step();
+        ++steps;
+      }
+    }
+    check_launch("time step");
+  }
+  int64_t per_step_launches = 0;
+
+  void drop_graph() {
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+  }
+
+  // DY2 v for history levels whose v was replaced from the host.
+  void recompute_dirty_q() {
+    for (int sl = 0; sl < 3; ++sl) {
+      if (!q_dirty[sl]) continue;
+      double2 *vv = v_ring + (size_t)sl * fs;
+      dapply(1, vv, tmpA);
+      dapply(2, vv, tmpB);
+      launch_combine_y(q_ring + (size_t)sl * fs, tmpA, c21, tmpB, c22, NY, M, st);
+      ++launches;
+      q_dirty[sl] = false;
+    }
+  }
+
+  void copy_ring(double2 *ring, size_t n, int from, int to) {
+    ck(cudaMemcpyAsync(ring + (size_t)to * n, ring + (size_t)from * n, n * sizeof(double2), cudaMemcpyDeviceToDevice,
+                       st), "ring copy");
+  }
+  // column of mode 0 of a device-layout field -> contiguous NY vector
+  void mode0_column(double2 *dst, const double2 *field) {
+    ck(cudaMemcpy2DAsync(dst, sizeof(double2), field, (size_t)M * sizeof(double2), sizeof(double2), NY,
+                         cudaMemcpyDeviceToDevice, st), "mode-0 column");
+  }
+
+  void get_vor_from_vel() {
+    dapply(1, u, tmpA);
+    dapply(1, w, tmpB);
+    VorArgs va{};
+    va.NY = NY; va.NXH = NXH; va.M = M; va.kx = kx; va.kz = kz; va.c11 = c11;
+    va.u = u; va.v = ring_level(v_ring, 0); va.w = w; va.d1u = tmpA; va.d1w = tmpB;
+    va.ox = ox; va.oy = ring_level(g_ring, 0); va.oz = oz;
+    launch_vor(va, st);
+    ++launches;
+  }
+  void lamb_vec(bool explicit_shift) {
+    launch_lamb(xform_args(), precision, st);
+    launches += 3;
+    if (explicit_shift) {
+      launch_lamb_mean_shift(lxm_ring, lzm_ring, lx, lz, NY, M, d_step, st);
+      ++launches;
+    }
+  }
+  void nonlinear_source(bool record_mean) {
+    launch_nl(nl_args(record_mean), st);
+    ++launches;
+  }
+  void friction(int shift) {
+    dapply(1, u, tmpA);
+    dapply(1, w, tmpB);
+    launch_friction(tmpA, tmpB, c11, NY, M, p.nu, Ly, fx_ring, fz_ring, d_step, shift, d_err, st);
+    ++launches;
+  }
+
+  void init_fields(const double *hu, const double *hv, const double *hw) {
+    steps = 0;
+    drop_graph();
+    ck(cudaMemsetAsync(d_step, 0, sizeof(long long), st), "memset");
+    ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "memset");
+    to_device(hu, u);
+    to_device(hv, ring_level(v_ring, 0));
+    to_device(hw, w);
+    get_vor_from_vel();  // also leaves D1 u, D1 w in tmpA, tmpB
+    launch_friction(tmpA, tmpB, c11, NY, M, p.nu, Ly, fx_ring, fz_ring, d_step, 0, d_err, st);
+    ++launches;
+    lamb_vec(false);
+    nonlinear_source(true);
+    const int s0 = slot(0);
+    for (double2 *ring : {v_ring, g_ring, hv_ring, hg_ring})
+      for (int l = 1; l < 3; ++l) copy_ring(ring, fs, s0, slot(l));
+    for (double2 *ring : {lxm_ring, lzm_ring})
+      for (int l = 1; l < 3; ++l) copy_ring(ring, NY, s0, slot(l));
+    mode0_column(U_ring + (size_t)s0 * NY, u);
+    mode0_column(W_ring + (size_t)s0 * NY, w);
+    for (double2 *ring : {U_ring, W_ring})
+      for (int l = 1; l < 3; ++l) copy_ring(ring, NY, s0, slot(l));
+    for (double *fr : {fx_ring, fz_ring})
+      for (int l = 1; l < 3; ++l)
+        ck(cudaMemcpyAsync(fr + slot(l), fr + s0, sizeof(double), cudaMemcpyDeviceToDevice, st), "fric copy");
+    q_dirty[0] = q_dirty[1] = q_dirty[2] = true;
+    recompute_dirty_q();
+    check_launch("init_fields");
+    initialized = true;
+  }
+
+  // ---- host <-> device in the reference layout ---------------------------------
+  void to_device(const double *host, double2 *dst) {
+    ck(cudaMemcpyAsync(stage, host, fs * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+    launch_transpose(stage, dst, M, NY, st);  // [M][NY] -> [NY][M]
+    ++launches;
+    check_launch("layout transpose");
+  }
+  void to_host(const double2 *src, double *host) {
+    launch_transpose(src, stage, NY, M, st);  // [NY][M] -> [M][NY]
+    ++launches;
+    check_launch("layout transpose");
+    ck(cudaMemcpyAsync(host, stage, fs * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "D2H");
+  }
+  double2 *field_ptr(int f, bool for_write) {
+    switch (f) {
+      case OWT_VELX: return u;
+      case OWT_VELZ: return w;
+      case OWT_VORX: return ox;
+      case OWT_VORZ: return oz;
+      case OWT_LMBX: return lx;
+      case OWT_LMBY: return ly;
+      case OWT_LMBZ: return lz;
+      case OWT_VELY: case OWT_VELY_0: case OWT_VELY_1: case OWT_VELY_2: {
+        const int l = f == OWT_VELY ? 0 : f - OWT_VELY_0;
+        if (for_write) q_dirty[slot(l)] = true;
+        return ring_level(v_ring, l);
+      }
+      case OWT_VORY: return ring_level(g_ring, 0);
+      case OWT_VORY_0: case OWT_VORY_1: case OWT_VORY_2: return ring_level(g_ring, f - OWT_VORY_0);
+      case OWT_HV: return ring_level(hv_ring, 0);
+      case OWT_HV_0: case OWT_HV_1: case OWT_HV_2: return ring_level(hv_ring, f - OWT_HV_0);
+      case OWT_HG: return ring_level(hg_ring, 0);
+      case OWT_HG_0: case OWT_HG_1: case OWT_HG_2: return ring_level(hg_ring, f - OWT_HG_0);
+      default: throw OwtError(OWT_ERR_INVALID, "unknown field id " + std::to_string(f));
+    }
+  }
+  double2 *mean_ptr(int which) {
+    if (which < 0 || which >= OWT_NUM_MEANS) throw OwtError(OWT_ERR_INVALID, "unknown mean id");
+    double2 *rings[4] = {lxm_ring, lzm_ring, U_ring, W_ring};
+    return rings[which / 3] + (size_t)slot(which % 3) * NY;
+  }
+  void sync_and_check() {
+    ck(cudaStreamSynchronize(st), "synchronize");
+    int e = 0;
+    ck(cudaMemcpy(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost), "status");
+    if (e == 2) throw OwtError(OWT_ERR_NUMERIC, "non-finite friction force: the state has blown up");
+    if (e) throw OwtError(OWT_ERR_NUMERIC, "device reported a numeric failure");
+  }
+};
+
+namespace {
+
+template <typename F>
+int guard(owt_handle *h, F &&f) {
+  if (!h) return OWT_ERR_INVALID;
+  try {
+    f();
+    h->err.clear();
+    return OWT_OK;
+  } catch (const OwtError &e) {
+    h->err = e.what();
+    return e.code;
+  } catch (const CudaError &e) {
+    h->err = e.what();
+    return OWT_ERR_CUDA;
+  } catch (const std::exception &e) {
+    h->err = e.what();
+    return OWT_ERR_INVALID;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int owt_create(const owt_params *params, owt_handle **out) {
+  if (!params || !out) {
+    g_create_error = "null argument";
+    return OWT_ERR_INVALID;
+  }
+  *out = nullptr;
+  owt_handle *h = new owt_handle();
+  try {
+    h->setup(*params);
+  } catch (const OwtError &e) {
+    g_create_error = e.what();
+    delete h;
+    return e.code;
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    delete h;
+    return dynamic_cast<const CudaError *>(&e) ? OWT_ERR_CUDA : OWT_ERR_INVALID;
+  }
+  *out = h;
+  return OWT_OK;
+}
+
+int owt_destroy(owt_handle *h) {
+  delete h;
+  return OWT_OK;
+}
+
+const char *owt_last_error(const owt_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int owt_init_fields(owt_handle *h, const double *velx, const double *vely, const double *velz) {
+  return guard(h, [&] {
+    if (!velx || !vely || !velz) throw OwtError(OWT_ERR_INVALID, "null field");
+    h->init_fields(velx, vely, velz);
+    h->sync_and_check();
+  });
+}
+
+int owt_time_integration(owt_handle *h, int64_t nsteps) {
+  return guard(h, [&] {
+    if (!h->initialized) throw OwtError(OWT_ERR_STATE, "owt_init_fields (or field uploads) must come first");
+    if (nsteps < 0) throw OwtError(OWT_ERR_INVALID, "negative step count");
+    h->run_steps(nsteps);
+  });
+}
+
+int owt_call(owt_handle *h, int routine) {
+  return guard(h, [&] {
+    switch (routine) {
+      case OWT_CALL_GET_VOR_FROM_VEL: h->get_vor_from_vel(); break;
+      case OWT_CALL_LAMB_VEC: h->lamb_vec(true); break;
+      case OWT_CALL_NONLINEAR_SOURCE: h->nonlinear_source(false); break;
+      case OWT_CALL_SOLVE_FRICTION_FORCE: h->friction(1); break;
+      case OWT_CALL_TIME_INTEGRATION:
+        if (!h->initialized) throw OwtError(OWT_ERR_STATE, "owt_init_fields (or field uploads) must come first");
+        h->run_steps(1);
+        break;
+      default: throw OwtError(OWT_ERR_INVALID, "unknown routine id");
+    }
+    h->check_launch("owt_call");
+    h->sync_and_check();
+  });
+}
+
+int owt_synchronize(owt_handle *h) {
+  return guard(h, [&] { h->sync_and_check(); });
+}
+
+int owt_get_field(owt_handle *h, int field, double *host) {
+  return guard(h, [&] {
+    if (!host) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    h->to_host(h->field_ptr(field, false), host);
+  });
+}
+
+int owt_set_field(owt_handle *h, int field, const double *host) {
+  return guard(h, [&] {
+    if (!host) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    h->to_device(host, h->field_ptr(field, true));
+    ck(cudaStreamSynchronize(h->st), "set field");
+    h->initialized = true;
+  });
+}
+
+int owt_get_mean(owt_handle *h, int which, double *host) {
+  return guard(h, [&] {
+    if (!host) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    ck(cudaMemcpyAsync(host, h->mean_ptr(which), h->NY * sizeof(double2), cudaMemcpyDeviceToHost, h->st), "D2H");
+    ck(cudaStreamSynchronize(h->st), "D2H");
+  });
+}
+
+int owt_set_mean(owt_handle *h, int which, const double *host) {
+  return guard(h, [&] {
+    if (!host) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    ck(cudaMemcpyAsync(h->mean_ptr(which), host, h->NY * sizeof(double2), cudaMemcpyHostToDevice, h->st), "H2D");
+    ck(cudaStreamSynchronize(h->st), "H2D");
+  });
+}
+
+int owt_get_friction(owt_handle *h, double *out6) {
+  return guard(h, [&] {
+    if (!out6) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    double fx[3], fz[3];
+    ck(cudaMemcpyAsync(fx, h->fx_ring, sizeof(fx), cudaMemcpyDeviceToHost, h->st), "D2H");
+    ck(cudaMemcpyAsync(fz, h->fz_ring, sizeof(fz), cudaMemcpyDeviceToHost, h->st), "D2H");
+    h->sync_and_check();
+    for (int l = 0; l < 3; ++l) {
+      out6[l] = fx[h->slot(l)];
+      out6[3 + l] = fz[h->slot(l)];
+    }
+  });
+}
+
+int owt_set_friction(owt_handle *h, const double *in6) {
+  return guard(h, [&] {
+    if (!in6) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    double fx[3], fz[3];
+    for (int l = 0; l < 3; ++l) {
+      fx[h->slot(l)] = in6[l];
+      fz[h->slot(l)] = in6[3 + l];
+    }
+    ck(cudaMemcpyAsync(h->fx_ring, fx, sizeof(fx), cudaMemcpyHostToDevice, h->st), "H2D");
+    ck(cudaMemcpyAsync(h->fz_ring, fz, sizeof(fz), cudaMemcpyHostToDevice, h->st), "H2D");
+    ck(cudaStreamSynchronize(h->st), "H2D");
+  });
+}
+
+int owt_set_precision(owt_handle *h, int precision) {
+  return guard(h, [&] {
+    if (precision != OWT_PREC_FP64 && precision != OWT_PREC_MIXED)
+      throw OwtError(OWT_ERR_INVALID, "precision must be OWT_PREC_FP64 or OWT_PREC_MIXED");
+    if (precision != h->precision) {
+      ck(cudaStreamSynchronize(h->st), "set precision");
+      h->drop_graph();
+      h->precision = precision;
+    }
+  });
+}
+
+int owt_use_graph(owt_handle *h, int on) {
+  return guard(h, [&] {
+    ck(cudaStreamSynchronize(h->st), "use graph");
+    if (!on) h->drop_graph();
+    h->use_graph = on != 0;
+  });
+}
+
+int owt_get_step(const owt_handle *h, int64_t *step) {
+  if (!h || !step) return OWT_ERR_INVALID;
+  *step = h->steps;
+  return OWT_OK;
+}
+
+int owt_get_stream(const owt_handle *h, void **stream) {
+  if (!h || !stream) return OWT_ERR_INVALID;
+  *stream = (void *)h->st;
+  return OWT_OK;
+}
+
+int owt_get_launch_count(const owt_handle *h, int64_t *count) {
+  if (!h || !count) return OWT_ERR_INVALID;
+  *count = h->launches;
+  return OWT_OK;
+}
+
+int owt_get_grid(const owt_handle *h, double *y) {
+  if (!h || !y) return OWT_ERR_INVALID;
+  std::memcpy(y, h->grid.y.data(), h->grid.y.size() * sizeof(double));
+  return OWT_OK;
+}
+
+int owt_enqueue_stage(owt_handle *h, int stage) {
+  return guard(h, [&] {
+    if (!h->initialized) throw OwtError(OWT_ERR_STATE, "owt_init_fields must come first");
+    switch (stage) {
+      case OWT_STAGE_MODES: h->stage_modes(); h->launches += 1; break;
+      case OWT_STAGE_MEAN: h->stage_mean(); h->launches += 1; break;
+      case OWT_STAGE_LAMB: h->launches += launch_lamb(h->xform_args(), h->precision, h->st); break;
+      case OWT_STAGE_NONLINEAR: launch_nl(h->nl_args(true), h->st); h->launches += 1; break;
+      default: throw OwtError(OWT_ERR_INVALID, "unknown stage");
+    }
+    h->check_launch("stage");
+  });
+}
+
+int owt_dy_apply(owt_handle *h, int order, const double *in, double *out) {
+  return guard(h, [&] {
+    if (order != 1 && order != 2) throw OwtError(OWT_ERR_INVALID, "order must be 1 or 2");
+    if (!in || !out) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    h->to_device(in, h->tmpC);
+    h->dapply(1, h->tmpC, h->tmpA);
+    if (order == 1) {
+      launch_combine_y(h->tmpB, h->tmpA, h->c11, nullptr, nullptr, h->NY, h->M, h->st);
+    } else {
+      h->dapply(2, h->tmpC, h->tmpB);
+      launch_combine_y(h->tmpB, h->tmpA, h->c21, h->tmpB, h->c22, h->NY, h->M, h->st);
+    }
+    ++h->launches;
+    h->check_launch("dy apply");
+    h->to_host(h->tmpB, out);
+  });
+}
+
+}  // extern "C"

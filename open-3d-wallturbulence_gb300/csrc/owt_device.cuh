@@ -1,0 +1,202 @@
+// Device building blocks shared by the transform and solve kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace owt {
+
+// Ring slot of history level 0 at step counter s (level l is (head + l) mod 3).
+__device__ __forceinline__ int ring_head(long long s) { return (int)((2 * (s % 3)) % 3); }
+
+// ---------------------------------------------------------------------------
+// Complex values: double2 / float2 with the arithmetic the kernels need.
+// ---------------------------------------------------------------------------
+template <typename T> struct cpx_t;
+template <> struct cpx_t<double> { using type = double2; };
+template <> struct cpx_t<float> { using type = float2; };
+template <typename T> using cpx = typename cpx_t<T>::type;
+
+template <typename T> __device__ __forceinline__ cpx<T> mk(T x, T y) { cpx<T> r; r.x = x; r.y = y; return r; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// a * b
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+__device__ __forceinline__ double2 to_d(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
+template <typename T> __device__ __forceinline__ cpx<T> from_d(double2 a);
+template <> __device__ __forceinline__ double2 from_d<double>(double2 a) { return a; }
+template <> __device__ __forceinline__ float2 from_d<float>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+
+// ---------------------------------------------------------------------------
+// FFT of many lines held in shared memory: self-sorting (Stockham) mixed-radix
+// schedule with radices 4, 2, 3.  At a stage of radix R after ns points have
+// been combined, butterfly j (of L/R) reads x[j + r L/R], multiplies by
+// w^(k r) with k = j mod ns and w = exp(sign 2 pi i / (ns R)), transforms, and
+// writes y[(j / ns) ns R + k + r ns].  Twiddles come from one table of
+// exp(-2 pi i m / L); the backward transform (sign +1) uses its conjugate.
+// Unnormalised in both directions, like FFTW.
+// ---------------------------------------------------------------------------
+struct FftPlan {
+  int L;
+  int nst;
+  int R[12];
+};
+
+template <typename T, bool BACKWARD>
+__device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx) {
+  cpx<T> w = tw[idx];
+  if (BACKWARD) w.y = -w.y;
+  return w;
+}
+
+template <typename T, bool BACKWARD>
+__device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, const FftPlan &p,
+                             const cpx<T> *__restrict__ tw) {
+  const int L = p.L;
+  int ns = 1;
+  for (int s = 0; s < p.nst; ++s) {
+    const int R = p.R[s];
+    const int nr = L / R;
+    const int step = L / (ns * R);
+    const int total = nlines * nr;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      const int line = idx / nr;
+      const int j = idx - line * nr;
+      const int k = j % ns;
+      const cpx<T> *src = a + line * lstride;
+      cpx<T> *dst = b + line * lstride;
+      const int base = (j - k) * R + k;
+      if (R == 4) {
+        cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
+        if (k != 0) {
+          x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
+          x2 = cmul(x2, twiddle<T, BACKWARD>(tw, 2 * k * step));
+          x3 = cmul(x3, twiddle<T, BACKWARD>(tw, 3 * k * step));
+        }
+        const cpx<T> t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
+        cpx<T> d = csub(x1, x3);
+        // t3 = d * (sign i): forward multiplies by -i, backward by +i
+        const cpx<T> t3 = BACKWARD ? mk<T>(-d.y, d.x) : mk<T>(d.y, -d.x);
+        dst[base] = cadd(t0, t2);
+        dst[base + ns] = cadd(t1, t3);
+        dst[base + 2 * ns] = csub(t0, t2);
+        dst[base + 3 * ns] = csub(t1, t3);
+      } else if (R == 2) {
+        cpx<T> x0 = src[j], x1 = src[j + nr];
+        if (k != 0) x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
+        dst[base] = cadd(x0, x1);
+        dst[base + ns] = csub(x0, x1);
+      } else {  // R == 3
+        cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
+        if (k != 0) {
+          x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
+          x2 = cmul(x2, twiddle<T, BACKWARD>(tw, 2 * k * step));
+        }
+        const T s60 = (T)0.86602540378443864676372317075294;
+        const cpx<T> t = cadd(x1, x2);
+        const cpx<T> d = csub(x1, x2);
+        const cpx<T> m = mk<T>(x0.x - (T)0.5 * t.x, x0.y - (T)0.5 * t.y);
+        // u = d * (sign i sin60)
+        const cpx<T> u = BACKWARD ? mk<T>(-s60 * d.y, s60 * d.x) : mk<T>(s60 * d.y, -s60 * d.x);
+        dst[base] = cadd(x0, t);
+        dst[base + ns] = cadd(m, u);
+        dst[base + 2 * ns] = csub(m, u);
+      }
+    }
+    __syncthreads();
+    cpx<T> *tmp = a; a = b; b = tmp;
+    ns *= R;
+  }
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// Banded LU solve, the algorithm of LAPACK dgbtrs ('N') on factors produced by
+// the dgbtf2 algorithm (see k_band_factor): forward sweep applying the row
+// interchanges and unit-lower multipliers column by column, then the upper
+// band back substitution.  Band storage AB[b][c][u] in LAPACK's factorization
+// layout (kv = KL + KU: row kv holds the diagonal, rows kv - t the t-th super-
+// diagonal of U, rows kv + t the multipliers of L), one system per unique
+// mode u, unique mode fastest so that neighbouring threads read neighbouring
+// words.  The diagonal row holds 1/U_jj (stored by the factorization).
+//
+// Each thread solves one complex right-hand side.  The active window of the
+// right-hand side lives in registers as a ring whose slot for entry j + t is
+// (s + t) mod W at unrolled step s, so all register indices are compile-time.
+//   rhs(p)      : entry p of the right-hand side (complex)
+//   ystore(p,v) : keep the forward-swept entry p (read back in reverse)
+//   yload(p)    : read it back
+//   out(c, x)   : solution entry for column c, produced for c = n-1 .. 0
+// ---------------------------------------------------------------------------
+template <int KL, int KU, class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
+                                           int U, int u, Rhs rhs, YStore ystore, YLoad yload, Out out) {
+  constexpr int KV = KL + KU;
+  constexpr int W = KL + 1;
+  const size_t sn = (size_t)n * U;  // stride between band rows
+  {
+    double2 w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : make_double2(0.0, 0.0);
+    for (int j0 = 0; j0 < n; j0 += W) {
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int j = j0 + s;
+        if (j < n) {
+          const int off = piv[(size_t)j * U + u];
+#pragma unroll
+          for (int t = 1; t < W; ++t) {
+            if (off == t) {
+              const double2 tmp = w[s];
+              w[s] = w[(s + t) % W];
+              w[(s + t) % W] = tmp;
+            }
+          }
+          const double2 yj = w[s];
+          ystore(j, yj);
+          const double *col = ab + (size_t)j * U + u;
+#pragma unroll
+          for (int t = 1; t < W; ++t) {
+            const double l = col[(size_t)(KV + t) * sn];
+            w[(s + t) % W].x -= l * yj.x;
+            w[(s + t) % W].y -= l * yj.y;
+          }
+          w[s] = (j + W < n) ? rhs(j + W) : make_double2(0.0, 0.0);
+        }
+      }
+    }
+  }
+  {
+    constexpr int WB = KV + 1;
+    double2 w[WB];
+#pragma unroll
+    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : make_double2(0.0, 0.0);
+    for (int jj = 0; jj < n; jj += WB) {
+#pragma unroll
+      for (int s = 0; s < WB; ++s) {
+        const int j = n - 1 - (jj + s);
+        if (j >= 0) {
+          const double *col = ab + (size_t)j * U + u;
+          const double rinv = col[(size_t)KV * sn];
+          const double2 x = make_double2(w[s].x * rinv, w[s].y * rinv);
+          out(j, x);
+#pragma unroll
+          for (int t = 1; t < WB; ++t) {
+            const double uu = col[(size_t)(KV - t) * sn];
+            w[(s + t) % WB].x -= uu * x.x;
+            w[(s + t) % WB].y -= uu * x.y;
+          }
+          w[s] = (j - WB >= 0) ? yload(j - WB) : make_double2(0.0, 0.0);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace owt

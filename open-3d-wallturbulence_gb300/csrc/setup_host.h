@@ -1,0 +1,88 @@
+// Host-side setup of the wall-normal discretisation for the GPU time step.
+//
+// Everything here is computed once per handle on the host in FP64 and then
+// uploaded: the stretched grid and metric (reference src/solver.cpp:57-106),
+// the compact finite-difference stencils (src/compdiff.hpp:11-357, as coded),
+// and the banded "augmented" forms of the two per-mode implicit systems.
+//
+// Augmented systems.  The reference solves, for every Fourier mode, the dense
+// systems Av v = r and Ag g = r (src/solver.cpp:577-603) whose matrices are
+// built from DYn = sum_m diag(c_nm) A_m^-1 B_m.  The same equations are banded
+// when the compact derivatives d_m = A_m^-1 B_m v are kept as unknowns:
+//
+//   v-system, 5 unknowns per node (v, d1, d2, d3, d4):
+//     A_m d_m - B_m v = 0                                  (m = 1..4, all rows)
+//     (a c21 - nu c41) d1 + (a c22 - nu c42) d2 - nu c43 d3 - nu c44 d4 - b v = r
+//                                  (rows 2..NY-3; a, b as in solver.cpp:577)
+//     v_0 = 0, c11_0 d1_0 = 0, c11_N-1 d1_N-1 = 0, v_N-1 = 0   (solver.cpp:581-596)
+//
+//   omega_y-system, reduced to 2 unknowns per node (d1, d2): with
+//   g_j = (r_j + nu c21_j d1_j + nu c22_j d2_j) / cg on interior nodes and
+//   g = 0 at the walls (solver.cpp:578, 588-599), cg = nu k^2 + gamma0/dt,
+//     A_m d_m - B_m g(d) = 0    (m = 1, 2)   i.e.   A_m d_m - (1/cg) B_m G d = (1/cg) B_m r
+//
+// The mean-mode solve of solve_mean (src/solver.cpp:448-485) is the
+// omega_y-system at k = 0, so it reuses that factorization.
+//
+// Equations are ordered by the midpoint of their column span (unknowns
+// interleaved by node); the resulting band widths are structural constants
+// (v-system kl = 18, ku = 15; omega_y-system kl = ku = 6) that the CUDA kernels
+// take as template parameters.  Band matrices are stored in LAPACK's
+// factorization layout (2kl+ku+1 rows, fill rows first) so that a partial-
+// pivoting band LU (the algorithm of LAPACK dgbtf2/dgbtrs) runs in place.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace owt {
+
+struct Grid {
+  int N = 0;
+  double ds = 0;
+  std::vector<double> s, y, dyds1, dyds2, dyds3, dyds4;
+  std::vector<double> c11, c21, c22, c31, c32, c33, c41, c42, c43, c44;
+};
+
+// Dense N x N row-major matrices of the stencils A_n, B_n (n = 1..4).
+struct Stencils {
+  int N = 0;
+  std::vector<double> A[4], B[4];
+  double a(int n, int i, int j) const { return A[n][(size_t)i * N + j]; }
+  double b(int n, int i, int j) const { return B[n][(size_t)i * N + j]; }
+};
+
+// One equation: coefficients on unknown columns, split as
+// value(k) = t0 + s1(k) * t1 + s2(k) * t2 with per-mode scalars s1, s2.
+struct Entry {
+  int col;
+  double t0, t1, t2;
+};
+
+// A banded system in template form, ordered and ready to be factored per mode.
+struct BandTemplate {
+  int n = 0;   // unknowns
+  int kl = 0, ku = 0;
+  int per_node = 0;
+  // [(kl+ku+1) x n]: entry (i, j) of the ordered matrix at row ku + i - j.
+  std::vector<double> t0, t1, t2;
+  // v-system: for each row position, the node whose r feeds it (-1: zero rhs).
+  std::vector<int> rhs_node;
+  // omega_y-system: rhs of row p = (1/cg) sum_e rb_val[p][e] * r[rb_col[p][e]].
+  std::vector<int> rb_col;     // [n x 5]
+  std::vector<double> rb_val;  // [n x 5]
+};
+
+Grid make_grid(int N, double alpha);
+Stencils make_stencils(int N, double h);
+BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu);
+BandTemplate build_g_system(const Grid &g, const Stencils &st, double nu);
+// Band LU (no per-mode scalars) of A_1, shared by every mode for DY1 f.
+BandTemplate build_plain_band(const Stencils &st, int which);
+
+// Twiddle table exp(-2 pi i k / L), k in [0, L), interleaved (re, im).
+std::vector<double> twiddles(int L);
+// Radix schedule for an FFT of length L = 2^a 3^b (4s first, then 2, then 3s).
+bool fft_radices(int L, std::vector<int> &radices);
+
+}  // namespace owt

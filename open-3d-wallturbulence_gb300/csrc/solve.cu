@@ -1,0 +1,525 @@
+// Per-mode wall-normal kernels of the time step (FP64 throughout).
+//
+// Device layout of a spectral field: [y][kz][kx] complex128, element
+// (j, k, i) at j*M + k*NXH + i with M = NZ*NXH, so the mode index m = k*NXH + i
+// is fastest and one thread per mode reads and writes coalesced rows.
+//
+// History levels (vely_0..2, vory_0..2, Hv_0..2, Hg_0..2 and the mean-mode
+// vectors, src/setup.hpp:64-79) live in three-slot rings; the reference's
+// deep-copy rotation (src/solver.cpp:612-626) becomes a step counter kept in
+// device memory: at counter s, level l is slot (2s + l) mod 3.  The counter
+// advances right after the mode kernel, so the new values written there
+// become level 0 and every later kernel of the step sees them as current.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "owt_device.cuh"
+#include "solve_kernels.h"
+
+namespace owt {
+
+// ---------------------------------------------------------------------------
+// Assemble and factor one banded system per unique mode (thread per mode).
+// value = t0 + s1[u] t1 + s2[u] t2; then LU with partial pivoting in the
+// order of LAPACK dgbtf2 (pivot: first entry of maximal magnitude within KL
+// rows; interchange across the current fill extent ju; scale; rank-1 update),
+// pivot offsets kept as bytes, and the diagonal replaced by its reciprocal.
+// ---------------------------------------------------------------------------
+template <int KL, int KU>
+__global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv, int n, int U,
+                              const double *__restrict__ t0, const double *__restrict__ t1,
+                              const double *__restrict__ t2, const double *__restrict__ s1,
+                              const double *__restrict__ s2, int *__restrict__ info) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= U) return;
+  constexpr int KV = KL + KU;
+  constexpr int NB = 2 * KL + KU + 1;
+  const size_t sn = (size_t)n * U;
+  auto AB = [&](int b, int c) -> double & { return ab[(size_t)b * sn + (size_t)c * U + u]; };
+  const double a1 = s1 ? s1[u] : 0.0, a2 = s2 ? s2[u] : 0.0;
+  for (int c = 0; c < n; ++c)
+    for (int b = 0; b < NB; ++b) {
+      double v = 0.0;
+      if (b >= KL) {
+        const size_t at = (size_t)(b - KL) * n + c;
+        v = t0[at] + a1 * t1[at] + a2 * t2[at];
+      }
+      AB(b, c) = v;
+    }
+  int ju = 0;
+  for (int j = 0; j < n; ++j) {
+    const int km = min(KL, n - 1 - j);
+    int jp = 0;
+    double best = fabs(AB(KV, j));
+    for (int i = 1; i <= km; ++i) {
+      const double v = fabs(AB(KV + i, j));
+      if (v > best) { best = v; jp = i; }
+    }
+    piv[(size_t)j * U + u] = (uint8_t)jp;
+    if (AB(KV + jp, j) == 0.0) {
+      atomicMax(info, 1);
+      continue;
+    }
+    ju = max(ju, min(j + KU + jp, n - 1));
+    if (jp != 0)
+      for (int c = j; c <= ju; ++c) {
+        double &x = AB(KV + jp - (c - j), c);
+        double &y = AB(KV - (c - j), c);
+        const double t = x; x = y; y = t;
+      }
+    const double rp = 1.0 / AB(KV, j);
+    for (int i = 1; i <= km; ++i) AB(KV + i, j) *= rp;
+    for (int c = j + 1; c <= ju; ++c) {
+      const double t = AB(KV - (c - j), c);
+      if (t != 0.0)
+        for (int i = 1; i <= km; ++i) AB(KV + i - (c - j), c) -= AB(KV + i, j) * t;
+    }
+  }
+  for (int j = 0; j < n; ++j) AB(KV, j) = 1.0 / AB(KV, j);
+}
+
+void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0,
+                        const double *t1, const double *t2, const double *s1, const double *s2, int *info,
+                        cudaStream_t st) {
+  const int bs = 64, gs = (U + bs - 1) / bs;
+  if (kl == 18 && ku == 15) k_band_factor<18, 15><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
+  else if (kl == 6 && ku == 6) k_band_factor<6, 6><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
+  else if (kl == 2 && ku == 2) k_band_factor<2, 2><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
+}
+
+bool band_supported(int kl, int ku) {
+  return (kl == 18 && ku == 15) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
+}
+
+// ---------------------------------------------------------------------------
+// Mode kernel: one thread per Fourier mode.  For mode (kz, kx):
+//  1. source_g = sum beta Hg_l + sum alpha g_l / dt      (solver.cpp:573-574)
+//  2. omega_y-system: g and DY1 g                         (solver.cpp:578, 603)
+//  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
+//     with DY2 v_l kept as a history of its own (q_l)    (solver.cpp:569-571)
+//  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
+//  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
+// ---------------------------------------------------------------------------
+template <int KLV, int KUV, int KLG, int KUG>
+__global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.M) return;
+  const int M = a.M, NY = a.NY;
+  const int k = m / a.NXH, i = m - k * a.NXH;
+  const int kabs = (k <= a.NZH) ? k : a.NZ - k;
+  const int u = kabs * a.NXH + i;
+  const double kx = a.kx[i], kz = a.kz[k];
+  const double k2 = kx * kx + kz * kz;
+  const long long s = *a.step;
+  const int h = ring_head(s);
+  const size_t fs = (size_t)NY * M;
+  const double2 *v0 = a.v_ring + (size_t)h * fs, *v1 = a.v_ring + (size_t)((h + 1) % 3) * fs,
+                *v2 = a.v_ring + (size_t)((h + 2) % 3) * fs;
+  const double2 *g0 = a.g_ring + (size_t)h * fs, *g1 = a.g_ring + (size_t)((h + 1) % 3) * fs,
+                *g2 = a.g_ring + (size_t)((h + 2) % 3) * fs;
+  const double2 *hv0 = a.hv_ring + (size_t)h * fs, *hv1 = a.hv_ring + (size_t)((h + 1) % 3) * fs,
+                *hv2 = a.hv_ring + (size_t)((h + 2) % 3) * fs;
+  const double2 *hg0 = a.hg_ring + (size_t)h * fs, *hg1 = a.hg_ring + (size_t)((h + 1) % 3) * fs,
+                *hg2 = a.hg_ring + (size_t)((h + 2) % 3) * fs;
+  const double2 *q0 = a.q_ring + (size_t)h * fs, *q1 = a.q_ring + (size_t)((h + 1) % 3) * fs,
+                *q2 = a.q_ring + (size_t)((h + 2) % 3) * fs;
+  const int hn = (h + 2) % 3;  // slot of the new level 0
+  double2 *vn = a.v_ring + (size_t)hn * fs;
+  double2 *gn = a.g_ring + (size_t)hn * fs;
+  double2 *qn = a.q_ring + (size_t)hn * fs;
+  const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
+  const double idt = a.inv_dt;
+
+  // 1. source_g, walls zero (solver.cpp:598-599)
+  for (int j = 0; j < NY; ++j) {
+    const size_t at = (size_t)j * M + m;
+    double2 r = make_double2(0.0, 0.0);
+    if (j != 0 && j != NY - 1) {
+      const double2 x0 = hg0[at], x1 = hg1[at], x2 = hg2[at];
+      const double2 y0 = g0[at], y1 = g1[at], y2 = g2[at];
+      r.x = (x0.x * be0 + x1.x * be1 + x2.x * be2) + (y0.x * al0 + y1.x * al1 + y2.x * al2) * idt;
+      r.y = (x0.y * be0 + x1.y * be1 + x2.y * be2) + (y0.y * al0 + y1.y * al1 + y2.y * al2) * idt;
+    }
+    a.sg[at] = r;
+  }
+
+  // 2. omega_y-system
+  const double icg = a.inv_cg[u];
+  {
+    double2 d2 = make_double2(0.0, 0.0);
+    auto rhs = [&](int p) -> double2 {
+      double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        const double b = a.rb_val[p * 5 + e];
+        const double2 r = a.sg[(size_t)a.rb_col[p * 5 + e] * M + m];
+        acc.x += b * r.x;
+        acc.y += b * r.y;
+      }
+      return make_double2(acc.x * icg, acc.y * icg);
+    };
+    auto ys = [&](int p, double2 y) { a.yg[(size_t)p * M + m] = y; };
+    auto yl = [&](int p) -> double2 { return a.yg[(size_t)p * M + m]; };
+    auto out = [&](int c, double2 x) {
+      const int jn = c >> 1;
+      if (c & 1) {
+        d2 = x;
+      } else {
+        const size_t at = (size_t)jn * M + m;
+        double2 g = make_double2(0.0, 0.0);
+        if (jn != 0 && jn != NY - 1) {
+          const double2 r = a.sg[at];
+          const double w1 = a.nu * a.c21[jn], w2 = a.nu * a.c22[jn];
+          g.x = (r.x + w1 * x.x + w2 * d2.x) * icg;
+          g.y = (r.y + w1 * x.y + w2 * d2.y) * icg;
+        }
+        gn[at] = g;
+        const double c11 = a.c11[jn];
+        a.dg[at] = make_double2(c11 * x.x, c11 * x.y);
+      }
+    };
+    band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
+  }
+
+  // 3-5. v-system and the horizontal components
+  {
+    const double k2dt = k2 * idt;
+    const bool horiz = !(k2 < 1.e-8);
+    const double ik2 = horiz ? 1.0 / k2 : 0.0;
+    const double ax = kx * ik2, az = kz * ik2;
+    double2 d1 = make_double2(0.0, 0.0), d2 = make_double2(0.0, 0.0);
+    auto rhs = [&](int p) -> double2 {
+      const int j = a.rhs_node_v[p];
+      if (j < 0) return make_double2(0.0, 0.0);
+      const size_t at = (size_t)j * M + m;
+      const double2 h0 = hv0[at], h1 = hv1[at], h2 = hv2[at];
+      const double2 x0 = v0[at], x1 = v1[at], x2 = v2[at];
+      const double2 z0 = q0[at], z1 = q1[at], z2 = q2[at];
+      const double vsx = x0.x * al0 + x1.x * al1 + x2.x * al2, vsy = x0.y * al0 + x1.y * al1 + x2.y * al2;
+      const double qsx = z0.x * al0 + z1.x * al1 + z2.x * al2, qsy = z0.y * al0 + z1.y * al1 + z2.y * al2;
+      double2 r;
+      r.x = (h0.x * be0 + h1.x * be1 + h2.x * be2) - k2dt * vsx + qsx * idt;
+      r.y = (h0.y * be0 + h1.y * be1 + h2.y * be2) - k2dt * vsy + qsy * idt;
+      return r;
+    };
+    auto ys = [&](int p, double2 y) { a.yv[(size_t)p * M + m] = y; };
+    auto yl = [&](int p) -> double2 { return a.yv[(size_t)p * M + m]; };
+    auto out = [&](int c, double2 x) {
+      const int jn = c / 5, t = c - 5 * jn;
+      if (t == 2) {
+        d2 = x;
+      } else if (t == 1) {
+        d1 = x;
+      } else if (t == 0) {
+        const size_t at = (size_t)jn * M + m;
+        vn[at] = x;
+        const double c21 = a.c21[jn], c22 = a.c22[jn], c11 = a.c11[jn];
+        const double2 q = make_double2(c21 * d1.x + c22 * d2.x, c21 * d1.y + c22 * d2.y);
+        qn[at] = q;
+        if (horiz) {
+          const double2 dv = make_double2(c11 * d1.x, c11 * d1.y);
+          const double2 g = gn[at], dgv = a.dg[at];
+          // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
+          const double2 uu = make_double2(-ax * dv.y + az * g.y, ax * dv.x - az * g.x);
+          const double2 ww = make_double2(-ax * g.y - az * dv.y, ax * g.x + az * dv.x);
+          // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
+          const double kzk2 = kz * k2, kxk2 = kx * k2;
+          const double tx = kx * dgv.x + kz * q.x - kzk2 * x.x, ty = kx * dgv.y + kz * q.y - kzk2 * x.y;
+          const double sx = kz * dgv.x - kx * q.x + kxk2 * x.x, sy = kz * dgv.y - kx * q.y + kxk2 * x.y;
+          a.u_out[at] = uu;
+          a.w_out[at] = ww;
+          a.ox_out[at] = make_double2(-ty * ik2, tx * ik2);
+          a.oz_out[at] = make_double2(-sy * ik2, sx * ik2);
+        }
+      }
+    };
+    band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+  }
+}
+
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, cudaStream_t st) {
+  const int bs = 128, gs = (a.M + bs - 1) / bs;
+  if (klv == 18 && kuv == 15 && klg == 6 && kug == 6) k_modes<18, 15, 6, 6><<<gs, bs, 0, st>>>(a);
+}
+
+__global__ void k_advance(long long *step) { *step += 1; }
+void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>>>(step); }
+
+// ---------------------------------------------------------------------------
+// Mean mode (solve_mean + solve_friction_force, src/solver.cpp:306-327,
+// 428-514), run after the counter advanced: old level l is slot (h+1+l) mod 3
+// and the new values go to slot h.  Thread 0 solves for the mean streamwise
+// velocity U, thread 1 for W, each with the omega_y-system of mode (0, 0)
+// (the same matrix as solve_mean's A).
+// ---------------------------------------------------------------------------
+__global__ void k_mean(MeanArgs a) {
+  const int t = threadIdx.x;
+  const int NY = a.NY;
+  const int h = ring_head(*a.step);
+  const int o0 = (h + 1) % 3, o1 = (h + 2) % 3, o2 = h;
+  if (t < 2) {
+    double2 *U = (t == 0) ? a.U_ring : a.W_ring;
+    const double2 *L = (t == 0) ? a.lx_ring : a.lz_ring;
+    const double *F = (t == 0) ? a.fx_ring : a.fz_ring;
+    double2 *sg = a.scratch + (size_t)t * NY;
+    double2 *yy = a.scratch + 2 * (size_t)NY + (size_t)t * a.n_g;
+    double2 *dd = a.dy1 + (size_t)t * NY;
+    const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
+    const double f0 = F[o0], f1 = F[o1], f2 = F[o2];
+    for (int j = 0; j < NY; ++j) {
+      double2 r = make_double2(0.0, 0.0);
+      if (j != 0 && j != NY - 1) {
+        const double2 l0 = L[o0 * NY + j], l1 = L[o1 * NY + j], l2 = L[o2 * NY + j];
+        const double2 u0 = U[o0 * NY + j], u1 = U[o1 * NY + j], u2 = U[o2 * NY + j];
+        r.x = be0 * (l0.x + f0) + be1 * (l1.x + f1) + be2 * (l2.x + f2) +
+              (al0 * u0.x + al1 * u1.x + al2 * u2.x) * a.inv_dt;
+        r.y = be0 * l0.y + be1 * l1.y + be2 * l2.y + (al0 * u0.y + al1 * u1.y + al2 * u2.y) * a.inv_dt;
+      }
+      sg[j] = r;
+    }
+    const double icg = a.inv_cg0;
+    double2 d2 = make_double2(0.0, 0.0);
+    double2 *Un = U + (size_t)h * NY;
+    auto rhs = [&](int p) -> double2 {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int e = 0; e < 5; ++e) {
+        const double b = a.rb_val[p * 5 + e];
+        const double2 r = sg[a.rb_col[p * 5 + e]];
+        acc.x += b * r.x;
+        acc.y += b * r.y;
+      }
+      return make_double2(acc.x * icg, acc.y * icg);
+    };
+    auto ys = [&](int p, double2 y) { yy[p] = y; };
+    auto yl = [&](int p) -> double2 { return yy[p]; };
+    auto out = [&](int c, double2 x) {
+      const int jn = c >> 1;
+      if (c & 1) {
+        d2 = x;
+      } else {
+        double2 g = make_double2(0.0, 0.0);
+        if (jn != 0 && jn != NY - 1) {
+          const double2 r = sg[jn];
+          const double w1 = a.nu * a.c21[jn], w2 = a.nu * a.c22[jn];
+          g.x = (r.x + w1 * x.x + w2 * d2.x) * icg;
+          g.y = (r.y + w1 * x.y + w2 * d2.y) * icg;
+        }
+        Un[jn] = g;
+        const double c11 = a.c11[jn];
+        dd[jn] = make_double2(c11 * x.x, c11 * x.y);
+      }
+    };
+    band_solve<6, 6>(a.ab_g, a.piv_g, a.n_g, a.U, 0, rhs, ys, yl, out);
+  }
+  __syncthreads();
+  const double2 *dU = a.dy1, *dW = a.dy1 + NY;
+  if (t == 0) {
+    const double fx = -a.nu / a.Ly * (dU[NY - 1].x - dU[0].x);
+    const double fz = -a.nu / a.Ly * (dW[NY - 1].x - dW[0].x);
+    a.fx_ring[h] = fx;
+    a.fz_ring[h] = fz;
+    if (!isfinite(fx) || !isfinite(fz)) atomicMax(a.err, 2);
+  }
+  const double2 *Un = a.U_ring + (size_t)h * NY, *Wn = a.W_ring + (size_t)h * NY;
+  for (int j = t; j < NY; j += blockDim.x) {
+    const size_t at = (size_t)j * a.M;  // mode 0
+    a.u_field[at] = Un[j];
+    a.w_field[at] = Wn[j];
+    a.ox_field[at] = dW[j];
+    a.oz_field[at] = make_double2(-dU[j].x, -dU[j].y);
+  }
+}
+
+void launch_mean(const MeanArgs &a, cudaStream_t st) { k_mean<<<1, 128, 0, st>>>(a); }
+
+// ---------------------------------------------------------------------------
+// nonlinear_source (src/solver.cpp:240-260), one thread per mode:
+//   Hg = i kz lx - i kx lz,   Hv = -k^2 ly - c11 A1^-1 B1 (i kx lx + i kz lz)
+// written to the level-0 slot; the thread of mode (0, 0) also records the
+// new mean Lamb vector (src/solver.cpp:296-302).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_nl(NLArgs a) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.M) return;
+  const int M = a.M, NY = a.NY;
+  const int k = m / a.NXH, i = m - k * a.NXH;
+  const double kx = a.kx[i], kz = a.kz[k];
+  const double k2 = kx * kx + kz * kz;
+  const int h = ring_head(*a.step);
+  const size_t fs = (size_t)NY * M;
+  double2 *hv = a.hv_ring + (size_t)h * fs, *hg = a.hg_ring + (size_t)h * fs;
+  auto fval = [&](int j) -> double2 {
+    const double2 x = a.lx[(size_t)j * M + m], z = a.lz[(size_t)j * M + m];
+    return make_double2(-kx * x.y - kz * z.y, kx * x.x + kz * z.x);
+  };
+  for (int j = 0; j < NY; ++j) {
+    double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int e = 0; e < 5; ++e) {
+      const double b = a.b1_val[j * 5 + e];
+      if (b != 0.0) {
+        const double2 f = fval(a.b1_col[j * 5 + e]);
+        acc.x += b * f.x;
+        acc.y += b * f.y;
+      }
+    }
+    const size_t at = (size_t)j * M + m;
+    a.bf[at] = acc;
+    const double2 x = a.lx[at], z = a.lz[at];
+    hg[at] = make_double2(-kz * x.y + kx * z.y, kz * x.x - kx * z.x);
+  }
+  auto rhs = [&](int p) -> double2 { return a.bf[(size_t)p * M + m]; };
+  auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
+  auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
+  auto out = [&](int c, double2 d) {
+    const size_t at = (size_t)c * M + m;
+    const double2 ly = a.ly[at];
+    const double c11 = a.c11[c];
+    hv[at] = make_double2(-k2 * ly.x - c11 * d.x, -k2 * ly.y - c11 * d.y);
+  };
+  band_solve<2, 2>(a.ab1, a.piv1, NY, 1, 0, rhs, ys, yl, out);
+  if (m == 0 && a.lx_mean) {
+    for (int j = 0; j < NY; ++j) {
+      a.lx_mean[(size_t)h * NY + j] = a.lx[(size_t)j * M];
+      a.lz_mean[(size_t)h * NY + j] = a.lz[(size_t)j * M];
+    }
+  }
+}
+
+void launch_nl(const NLArgs &a, cudaStream_t st) {
+  const int bs = 128, gs = (a.M + bs - 1) / bs;
+  k_nl<<<gs, bs, 0, st>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// d = A_n^-1 B_n f along y for every mode (raw compact derivative on the
+// uniform s-grid; callers apply the metric).  Used at start-up and by the
+// DYn entry point, not in the step.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_dapply(DApplyArgs a) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.M) return;
+  const int M = a.M, NY = a.NY;
+  for (int j = 0; j < NY; ++j) {
+    double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int e = 0; e < 5; ++e) {
+      const double b = a.b_val[j * 5 + e];
+      if (b != 0.0) {
+        const double2 f = a.in[(size_t)a.b_col[j * 5 + e] * M + m];
+        acc.x += b * f.x;
+        acc.y += b * f.y;
+      }
+    }
+    a.bf[(size_t)j * M + m] = acc;
+  }
+  auto rhs = [&](int p) -> double2 { return a.bf[(size_t)p * M + m]; };
+  auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
+  auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
+  auto out = [&](int c, double2 d) { a.out[(size_t)c * M + m] = d; };
+  band_solve<2, 2>(a.ab, a.piv, NY, 1, 0, rhs, ys, yl, out);
+}
+
+void launch_dapply(const DApplyArgs &a, cudaStream_t st) {
+  const int bs = 128, gs = (a.M + bs - 1) / bs;
+  k_dapply<<<gs, bs, 0, st>>>(a);
+}
+
+// Elementwise helpers --------------------------------------------------------
+
+// out = sa * A + sb * B with per-y real coefficients (either may be null).
+__global__ void k_combine_y(double2 *out, const double2 *A, const double *ca, const double2 *B, const double *cb,
+                            int NY, int M) {
+  const size_t n = (size_t)NY * M;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e / M);
+    double2 r = make_double2(0.0, 0.0);
+    if (A) { r.x += ca[j] * A[e].x; r.y += ca[j] * A[e].y; }
+    if (B) { r.x += cb[j] * B[e].x; r.y += cb[j] * B[e].y; }
+    out[e] = r;
+  }
+}
+void launch_combine_y(double2 *out, const double2 *A, const double *ca, const double2 *B, const double *cb, int NY,
+                      int M, cudaStream_t st) {
+  k_combine_y<<<1024, 256, 0, st>>>(out, A, ca, B, cb, NY, M);
+}
+
+// get_vor_from_vel (src/solver.cpp:227-237) given D1 u and D1 w:
+//   vorx = c11 D1w - i kz v ; vory = i kz u - i kx w ; vorz = i kx v - c11 D1u
+__global__ void k_vor(VorArgs a) {
+  const size_t n = (size_t)a.NY * a.M;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e / a.M);
+    const int m = (int)(e - (size_t)j * a.M);
+    const int k = m / a.NXH, i = m - k * a.NXH;
+    const double kx = a.kx[i], kz = a.kz[k], c11 = a.c11[j];
+    const double2 u = a.u[e], v = a.v[e], w = a.w[e], du = a.d1u[e], dw = a.d1w[e];
+    a.ox[e] = make_double2(c11 * dw.x + kz * v.y, c11 * dw.y - kz * v.x);
+    a.oy[e] = make_double2(-kz * u.y + kx * w.y, kz * u.x - kx * w.x);
+    a.oz[e] = make_double2(-kx * v.y - c11 * du.x, kx * v.x - c11 * du.y);
+  }
+}
+void launch_vor(const VorArgs &a, cudaStream_t st) { k_vor<<<1024, 256, 0, st>>>(a); }
+
+// solve_friction_force (src/solver.cpp:306-327) from D1 u and D1 w of mode 0;
+// shift = 1 moves the history by explicit copies (stand-alone call), shift = 0
+// writes level 0 in place (start-up fills all levels afterwards).
+__global__ void k_friction(const double2 *d1u, const double2 *d1w, const double *c11, int NY, int M, double nu,
+                           double Ly, double *fx_ring, double *fz_ring, const long long *step, int shift, int *err) {
+  const int h = ring_head(*step);
+  const double dub = c11[0] * d1u[0].x, dut = c11[NY - 1] * d1u[(size_t)(NY - 1) * M].x;
+  const double dwb = c11[0] * d1w[0].x, dwt = c11[NY - 1] * d1w[(size_t)(NY - 1) * M].x;
+  const double fx = -nu / Ly * (dut - dub), fz = -nu / Ly * (dwt - dwb);
+  if (shift) {
+    const int l0 = h, l1 = (h + 1) % 3, l2 = (h + 2) % 3;
+    fx_ring[l2] = fx_ring[l1]; fx_ring[l1] = fx_ring[l0];
+    fz_ring[l2] = fz_ring[l1]; fz_ring[l1] = fz_ring[l0];
+  }
+  fx_ring[h] = fx;
+  fz_ring[h] = fz;
+  if (!isfinite(fx) || !isfinite(fz)) atomicMax(err, 2);
+}
+void launch_friction(const double2 *d1u, const double2 *d1w, const double *c11, int NY, int M, double nu, double Ly,
+                     double *fx_ring, double *fz_ring, const long long *step, int shift, int *err, cudaStream_t st) {
+  k_friction<<<1, 1, 0, st>>>(d1u, d1w, c11, NY, M, nu, Ly, fx_ring, fz_ring, step, shift, err);
+}
+
+// Mean Lamb history shift by copies, as Lamb_vec does it (src/solver.cpp:296-302).
+__global__ void k_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY,
+                                  int M, const long long *step) {
+  const int h = ring_head(*step), l1 = (h + 1) % 3, l2 = (h + 2) % 3;
+  for (int j = threadIdx.x; j < NY; j += blockDim.x) {
+    lx_ring[l2 * NY + j] = lx_ring[l1 * NY + j];
+    lx_ring[l1 * NY + j] = lx_ring[h * NY + j];
+    lx_ring[h * NY + j] = lx[(size_t)j * M];
+    lz_ring[l2 * NY + j] = lz_ring[l1 * NY + j];
+    lz_ring[l1 * NY + j] = lz_ring[h * NY + j];
+    lz_ring[h * NY + j] = lz[(size_t)j * M];
+  }
+}
+void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
+                            const long long *step, cudaStream_t st) {
+  k_lamb_mean_shift<<<1, 256, 0, st>>>(lx_ring, lz_ring, lx, lz, NY, M, step);
+}
+
+// Reference layout [z][x][y] <-> device layout [y][z][x]: a transpose of an
+// M x NY matrix of complex128 through 32 x 32 shared-memory tiles.
+__global__ void k_transpose(const double2 *__restrict__ in, double2 *__restrict__ out, int rows, int cols) {
+  __shared__ double2 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = by + r, col = bx + threadIdx.x;
+    if (row < rows && col < cols) tile[r][threadIdx.x] = in[(size_t)row * cols + col];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int orow = bx + r, ocol = by + threadIdx.x;
+    if (orow < cols && ocol < rows) out[(size_t)orow * rows + ocol] = tile[threadIdx.x][r];
+  }
+}
+void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st) {
+  dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose<<<g, b, 0, st>>>(in, out, rows, cols);
+}
+
+}  // namespace owt

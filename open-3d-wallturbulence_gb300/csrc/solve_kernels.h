@@ -1,0 +1,114 @@
+// Argument blocks and launchers of the per-mode kernels (solve.cu) and the
+// transform kernels (transforms.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "owt_device.cuh"
+
+namespace owt {
+
+struct ModeArgs {
+  int NY, NZ, NXH, NZH, M, U;
+  double inv_dt, nu;
+  const double *kx, *kz, *c11, *c21, *c22;
+  double2 *v_ring, *g_ring, *hv_ring, *hg_ring, *q_ring;  // 3 slots each, [slot][y][mode]
+  double2 *u_out, *w_out, *ox_out, *oz_out;
+  const double *ab_v; const uint8_t *piv_v; int n_v;
+  const double *ab_g; const uint8_t *piv_g; int n_g;
+  const int *rhs_node_v;
+  const int *rb_col; const double *rb_val;
+  const double *inv_cg;
+  double2 *sg, *dg, *yv, *yg;  // scratch
+  const long long *step;
+};
+
+struct MeanArgs {
+  int NY, M, U, n_g;
+  double inv_dt, nu, Ly, inv_cg0;
+  const double *c11, *c21, *c22;
+  const double *ab_g; const uint8_t *piv_g;
+  const int *rb_col; const double *rb_val;
+  double2 *U_ring, *W_ring, *lx_ring, *lz_ring;  // [3][NY]
+  double *fx_ring, *fz_ring;                     // [3]
+  double2 *u_field, *w_field, *ox_field, *oz_field;
+  double2 *scratch;  // 2*NY + 2*n_g
+  double2 *dy1;      // 2*NY
+  const long long *step;
+  int *err;
+};
+
+struct NLArgs {
+  int NY, NZ, NXH, M;
+  const double *kx, *kz, *c11;
+  const double2 *lx, *ly, *lz;
+  double2 *hv_ring, *hg_ring;
+  const double *ab1; const uint8_t *piv1;
+  const int *b1_col; const double *b1_val;
+  double2 *bf, *yscr;
+  double2 *lx_mean, *lz_mean;  // rings [3][NY], or null
+  const long long *step;
+};
+
+struct DApplyArgs {
+  int NY, M;
+  const double2 *in;
+  double2 *out;
+  const double *ab; const uint8_t *piv;
+  const int *b_col; const double *b_val;
+  double2 *bf, *yscr;
+};
+
+struct VorArgs {
+  int NY, NXH, M;
+  const double *kx, *kz, *c11;
+  const double2 *u, *v, *w, *d1u, *d1w;
+  double2 *ox, *oy, *oz;
+};
+
+// Transform kernels: inputs for the inverse pass are six spectral fields
+// (u, v, w, omega_x, omega_y, omega_z) in device layout; outputs three.
+struct XformDims {
+  int NY, NZ, NXH, NZH, NX2, NZ2;
+};
+struct XformArgs {
+  XformDims d;
+  // in[f] is a plain field, or (bit f of ring_mask set) the base of a
+  // three-slot ring whose level-0 slot is chosen from the step counter.
+  const double2 *in[6];
+  int ring_mask;
+  size_t fs;
+  const long long *step;
+  double2 *out[3];
+  void *zbuf;  // [6][NY][NZ2][NXH] complex<T>
+  void *lbuf;  // [3][NY][NZ2][NXH] complex<T>
+  FftPlan px, pz;
+  const void *twx, *twz;  // tables of exp(-2 pi i k/L) in T precision
+  double inv_nx2, inv_nz2;
+};
+
+bool band_supported(int kl, int ku);
+void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0, const double *t1,
+                        const double *t2, const double *s1, const double *s2, int *info, cudaStream_t st);
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, cudaStream_t st);
+void launch_advance(long long *step, cudaStream_t st);
+void launch_mean(const MeanArgs &a, cudaStream_t st);
+void launch_nl(const NLArgs &a, cudaStream_t st);
+void launch_dapply(const DApplyArgs &a, cudaStream_t st);
+void launch_combine_y(double2 *out, const double2 *A, const double *ca, const double2 *B, const double *cb, int NY,
+                      int M, cudaStream_t st);
+void launch_vor(const VorArgs &a, cudaStream_t st);
+void launch_friction(const double2 *d1u, const double2 *d1w, const double *c11, int NY, int M, double nu, double Ly,
+                     double *fx_ring, double *fz_ring, const long long *step, int shift, int *err, cudaStream_t st);
+void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
+                            const long long *step, cudaStream_t st);
+void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st);
+
+// Lamb vector: z-backward (6 fields) -> x pass with products -> z-forward (3).
+// precision 0: FP64, 1: FP32 transforms and products.  Returns launches issued.
+int launch_lamb(const XformArgs &a, int precision, cudaStream_t st);
+cudaError_t lamb_prepare(const XformDims &d);
+size_t lamb_zbuf_bytes(const XformDims &d, int precision);
+size_t lamb_lbuf_bytes(const XformDims &d, int precision);
+
+}  // namespace owt

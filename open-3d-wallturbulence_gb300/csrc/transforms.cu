@@ -1,0 +1,216 @@
+// Dealiased transforms and the Lamb vector (src/solver.cpp:262-304,
+// src/FFT.cpp:49-194) as three kernels that never write a padded 3/2-grid
+// physical field to memory:
+//
+//  k_zback : per (y, kx tile, field) -- gather kz into the padded z line
+//            (k < NZH -> slot k, k > NZH -> slot k + NZH, the Nyquist row
+//            k = NZH dropped, FFT.cpp:78-87), backward FFT of length NZ2.
+//  k_xlamb : per (y, z) line pair -- Hermitian extension in x (slot i = u_i,
+//            slot NX + i = conj(u_{NXH-i}), FFT.cpp:109-119) with two real
+//            fields packed into one complex backward FFT of length NX2 (the
+//            real part of the reference's c2c output is exactly such a c2r,
+//            with Im u_0 ignored), the cross product u x omega in physical
+//            space (solver.cpp:284-286, no fused multiply-add), two real
+//            products packed into one forward FFT, keep kx < NXH, / NX2
+//            (FFT.cpp:153-162).
+//  k_zfwd  : per (y, kx tile, field) -- forward FFT of length NZ2, keep slots
+//            k < NZH and NZ + k (k < NZH) -> kz index k + NZH, / NZ2
+//            (FFT.cpp:177-188).  The Nyquist row is kept on this path.
+//
+// Between kernels the z-padded, x-truncated planes live in HBM as
+// [field][y][z][kx] complex<T>.  T = double (FP64 step) or float (mixed).
+#include <cuda_runtime.h>
+
+#include "owt_device.cuh"
+#include "solve_kernels.h"
+
+namespace owt {
+
+template <typename T> struct XCfg;
+template <> struct XCfg<double> { static constexpr int TX = 4; static constexpr int P = 2; };
+template <> struct XCfg<float> { static constexpr int TX = 8; static constexpr int P = 4; };
+
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zback(XformArgs a) {
+  constexpr int TX = XCfg<T>::TX;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const XformDims d = a.d;
+  const int ls = d.NZ2 + 1;
+  cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
+  cpx<T> *bufb = bufa + TX * ls;
+  const int i0 = blockIdx.x * TX, j = blockIdx.y, f = blockIdx.z;
+  const int M = d.NZ * d.NXH;
+  const double2 *base = a.in[f];
+  if (a.ring_mask & (1 << f)) base += (size_t)ring_head(*a.step) * a.fs;
+  const double2 *src = base + (size_t)j * M;
+  for (int idx = threadIdx.x; idx < TX * ls; idx += blockDim.x) bufa[idx] = mk<T>((T)0, (T)0);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
+    const int kz = idx / TX, c = idx - kz * TX;
+    if (i0 + c < d.NXH && kz != d.NZH) {
+      const int slot = kz < d.NZH ? kz : kz + d.NZH;
+      bufa[c * ls + slot] = from_d<T>(src[(size_t)kz * d.NXH + i0 + c]);
+    }
+  }
+  __syncthreads();
+  const cpx<T> *r = fft_lines<T, true>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
+  cpx<T> *dst = reinterpret_cast<cpx<T> *>(a.zbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
+  for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
+    const int z = idx / TX, c = idx - z * TX;
+    if (i0 + c < d.NXH) dst[(size_t)z * d.NXH + i0 + c] = r[c * ls + z];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_xlamb(XformArgs a) {
+  constexpr int P = XCfg<T>::P;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const XformDims d = a.d;
+  const int ls = d.NX2 + 1;
+  cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
+  cpx<T> *bufb = bufa + 3 * P * ls;
+  const size_t nlines = (size_t)d.NY * d.NZ2;
+  const size_t line0 = (size_t)blockIdx.x * P;
+  const size_t fstride = nlines * d.NXH;
+  const cpx<T> *zb = reinterpret_cast<const cpx<T> *>(a.zbuf);
+  // 1. pack field pairs (u,v), (w,ox), (oy,oz) into complex spectra
+  for (int idx = threadIdx.x; idx < 3 * P * d.NX2; idx += blockDim.x) {
+    const int q = idx / d.NX2, mm = idx - q * d.NX2;
+    const int pair = q / P, l = q - pair * P;
+    const size_t line = line0 + l;
+    cpx<T> z = mk<T>((T)0, (T)0);
+    if (line < nlines) {
+      const cpx<T> *A = zb + (size_t)(2 * pair) * fstride + line * d.NXH;
+      const cpx<T> *B = A + fstride;
+      if (mm == 0) {
+        z = mk<T>(A[0].x, B[0].x);
+      } else if (mm < d.NXH) {
+        const cpx<T> x = A[mm], y = B[mm];
+        z = mk<T>(x.x - y.y, x.y + y.x);
+      } else if (mm > d.NX2 - d.NXH) {
+        const int mp = d.NX2 - mm;
+        const cpx<T> x = A[mp], y = B[mp];
+        z = mk<T>(x.x + y.y, y.x - x.y);
+      }
+    }
+    bufa[q * ls + mm] = z;
+  }
+  __syncthreads();
+  const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.twx);
+  cpx<T> *r = fft_lines<T, true>(bufa, bufb, 3 * P, ls, a.px, tw);
+  cpx<T> *o = (r == bufa) ? bufb : bufa;
+  // 2. lamb = u x omega, packed as (lx + i ly) per line and (lz_l + i lz_l+1)
+  for (int idx = threadIdx.x; idx < P * d.NX2; idx += blockDim.x) {
+    const int l = idx / d.NX2, x = idx - l * d.NX2;
+    const cpx<T> uv = r[(0 * P + l) * ls + x], wox = r[(1 * P + l) * ls + x], oyz = r[(2 * P + l) * ls + x];
+    const T u = uv.x, v = uv.y, w = wox.x, ox = wox.y, oy = oyz.x, oz = oyz.y;
+    const T lx = mul_rn(v, oz) - mul_rn(w, oy);
+    const T ly = mul_rn(w, ox) - mul_rn(u, oz);
+    const T lz = mul_rn(u, oy) - mul_rn(v, ox);
+    o[l * ls + x] = mk<T>(lx, ly);
+    if (l & 1) o[(P + l / 2) * ls + x].y = lz;
+    else o[(P + l / 2) * ls + x].x = lz;
+  }
+  __syncthreads();
+  cpx<T> *fo = fft_lines<T, false>(o, r, P + P / 2, ls, a.px, tw);
+  // 3. unpack the real-pair spectra, keep kx < NXH, scale by 1/NX2
+  cpx<T> *lb = reinterpret_cast<cpx<T> *>(a.lbuf);
+  const T half = (T)(0.5 * a.inv_nx2);
+  for (int idx = threadIdx.x; idx < P * d.NXH; idx += blockDim.x) {
+    const int l = idx / d.NXH, mm = idx - l * d.NXH;
+    const size_t line = line0 + l;
+    if (line >= nlines) continue;
+    const int mc = (mm == 0) ? 0 : d.NX2 - mm;
+    {
+      const cpx<T> zm = fo[l * ls + mm], zc = fo[l * ls + mc];
+      // Xa = (Z[m] + conj Z[-m]) / 2 ; Xb = (Z[m] - conj Z[-m]) / (2i)
+      lb[line * d.NXH + mm] = mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
+      lb[fstride + line * d.NXH + mm] = mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half);
+    }
+    {
+      const cpx<T> zm = fo[(P + l / 2) * ls + mm], zc = fo[(P + l / 2) * ls + mc];
+      const cpx<T> val = (l & 1) ? mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half)
+                                 : mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
+      lb[2 * fstride + line * d.NXH + mm] = val;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zfwd(XformArgs a) {
+  constexpr int TX = XCfg<T>::TX;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const XformDims d = a.d;
+  const int ls = d.NZ2 + 1;
+  cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
+  cpx<T> *bufb = bufa + TX * ls;
+  const int i0 = blockIdx.x * TX, j = blockIdx.y, f = blockIdx.z;
+  const cpx<T> *src = reinterpret_cast<const cpx<T> *>(a.lbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
+  for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
+    const int z = idx / TX, c = idx - z * TX;
+    bufa[c * ls + z] = (i0 + c < d.NXH) ? src[(size_t)z * d.NXH + i0 + c] : mk<T>((T)0, (T)0);
+  }
+  __syncthreads();
+  const cpx<T> *r = fft_lines<T, false>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
+  double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
+  const double sc = a.inv_nz2;
+  for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
+    const int kz = idx / TX, c = idx - kz * TX;
+    if (i0 + c < d.NXH) {
+      const int slot = kz < d.NZH ? kz : kz + d.NZH;
+      const double2 v = to_d(r[c * ls + slot]);
+      dst[(size_t)kz * d.NXH + i0 + c] = make_double2(v.x * sc, v.y * sc);
+    }
+  }
+}
+
+template <typename T>
+static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * (d.NZ2 + 1) * sizeof(cpx<T>); }
+template <typename T>
+static size_t smem_x(const XformDims &d) { return 2 * 3 * (size_t)XCfg<T>::P * (d.NX2 + 1) * sizeof(cpx<T>); }
+
+template <typename T>
+static int lamb_t(const XformArgs &a, cudaStream_t st) {
+  const XformDims &d = a.d;
+  constexpr int TX = XCfg<T>::TX, P = XCfg<T>::P;
+  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  dim3 gz((d.NXH + TX - 1) / TX, d.NY, 6);
+  k_zback<T><<<gz, 256, sz, st>>>(a);
+  const size_t nl = (size_t)d.NY * d.NZ2;
+  k_xlamb<T><<<(unsigned)((nl + P - 1) / P), 256, sx, st>>>(a);
+  dim3 gf((d.NXH + TX - 1) / TX, d.NY, 3);
+  k_zfwd<T><<<gf, 256, sz, st>>>(a);
+  return 3;
+}
+
+template <typename T>
+static cudaError_t prepare_t(const XformDims &d) {
+  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  cudaError_t e = cudaFuncSetAttribute(k_zback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_zfwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_xlamb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
+  return e;
+}
+
+// Opt the transform kernels in to the dynamic shared memory they need; called
+// once per handle, before any launch or graph capture.
+cudaError_t lamb_prepare(const XformDims &d) {
+  cudaError_t e = prepare_t<double>(d);
+  return e == cudaSuccess ? prepare_t<float>(d) : e;
+}
+
+int launch_lamb(const XformArgs &a, int precision, cudaStream_t st) {
+  return precision == 0 ? lamb_t<double>(a, st) : lamb_t<float>(a, st);
+}
+
+size_t lamb_zbuf_bytes(const XformDims &d, int precision) {
+  return 6 * (size_t)d.NY * d.NZ2 * d.NXH * (precision == 0 ? sizeof(double2) : sizeof(float2));
+}
+size_t lamb_lbuf_bytes(const XformDims &d, int precision) {
+  return 3 * (size_t)d.NY * d.NZ2 * d.NXH * (precision == 0 ? sizeof(double2) : sizeof(float2));
+}
+
+}  // namespace owt

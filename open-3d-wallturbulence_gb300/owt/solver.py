@@ -1,0 +1,161 @@
+"""GPU channel-DNS solver with the reference's routine names.
+
+The reference is a set of free functions on C++ globals (src/setup.hpp:84-114)
+driven by src/main.cpp:63-87.  ``GpuSolver`` keeps those names and their
+meaning on one device-resident state:
+
+    s = GpuSolver(params)                      # allocate_var + init_mat + init_fft
+    s.init_fields(velx, vely, velz)            # init_fields with a given velocity
+    for step in range(NT + 1):
+        s.time_Integration()                   # time_Integration
+    s.get("vely")                              # the global vely, [z][x][y]
+
+Arrays are numpy complex128 in the reference Field layout [z][x][y].
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as _L
+from .params import CaseParams
+
+
+class GpuSolver:
+    def __init__(self, params: CaseParams, precision="fp64", device=0):
+        self.L = _L.load()
+        self.params = params
+        p = _L.OwtParams(params.dt, params.dkx, params.dkz, params.alpha_mesh, params.nu, params.NX, params.NY,
+                         params.NZ, _L.PREC[precision], device)
+        h = C.c_void_p()
+        rc = self.L.owt_create(C.byref(p), C.byref(h))
+        if rc != _L.OK:
+            raise _L.OwtError(rc, self.L.owt_last_error(None).decode())
+        self.h = h
+        self.shape = params.spectral_shape
+
+    # -- plumbing -------------------------------------------------------------
+    def _chk(self, rc):
+        if rc != _L.OK:
+            raise _L.OwtError(rc, self.L.owt_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.owt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, a):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        if a.shape != self.shape:
+            raise ValueError(f"expected shape {self.shape}, got {a.shape}")
+        return a
+
+    # -- reference routines -----------------------------------------------------
+    def init_fields(self, velx, vely, velz):
+        u, v, w = self._c(velx), self._c(vely), self._c(velz)
+        self._chk(self.L.owt_init_fields(self.h, *[_L.dptr(x.view(np.float64)) for x in (u, v, w)]))
+
+    def time_Integration(self, nsteps=1):
+        self._chk(self.L.owt_time_integration(self.h, int(nsteps)))
+
+    def call(self, routine):
+        self._chk(self.L.owt_call(self.h, _L.ROUTINES[routine]))
+
+    def get_vor_from_vel(self):
+        self.call("get_vor_from_vel")
+
+    def Lamb_vec(self):
+        self.call("Lamb_vec")
+
+    def nonlinear_source(self):
+        self.call("nonlinear_source")
+
+    def solve_friction_force(self):
+        self.call("solve_friction_force")
+
+    def synchronize(self):
+        self._chk(self.L.owt_synchronize(self.h))
+
+    # -- state access -----------------------------------------------------------
+    def get(self, name, out=None):
+        out = np.empty(self.shape, np.complex128) if out is None else out
+        self._chk(self.L.owt_get_field(self.h, _L.FIELDS.index(name), _L.dptr(out.view(np.float64))))
+        return out
+
+    def set(self, name, arr):
+        a = self._c(arr)
+        self._chk(self.L.owt_set_field(self.h, _L.FIELDS.index(name), _L.dptr(a.view(np.float64))))
+
+    def get_cvec(self, name):
+        out = np.empty(self.params.NY, np.complex128)
+        self._chk(self.L.owt_get_mean(self.h, _L.MEANS.index(name), _L.dptr(out.view(np.float64))))
+        return out
+
+    def set_cvec(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.complex128)
+        self._chk(self.L.owt_set_mean(self.h, _L.MEANS.index(name), _L.dptr(a.view(np.float64))))
+
+    def friction(self):
+        out = np.empty(6)
+        self._chk(self.L.owt_get_friction(self.h, _L.dptr(out)))
+        return out
+
+    def set_friction(self, vals):
+        a = np.ascontiguousarray(vals, dtype=np.float64)
+        self._chk(self.L.owt_set_friction(self.h, _L.dptr(a)))
+
+    def get_scalar(self, name):
+        names = ["fx_fric_0", "fx_fric_1", "fx_fric_2", "fz_fric_0", "fz_fric_1", "fz_fric_2"]
+        return float(self.friction()[names.index(name)])
+
+    def state(self):
+        d = {n: self.get(n) for n in _L.FIELDS}
+        d.update({n: self.get_cvec(n) for n in _L.MEANS})
+        f = self.friction()
+        for q, n in enumerate(["fx_fric_0", "fx_fric_1", "fx_fric_2", "fz_fric_0", "fz_fric_1", "fz_fric_2"]):
+            d[n] = float(f[q])
+        return d
+
+    def dy(self, order, field):
+        a = self._c(field)
+        out = np.empty(self.shape, np.complex128)
+        self._chk(self.L.owt_dy_apply(self.h, int(order), _L.dptr(a.view(np.float64)), _L.dptr(out.view(np.float64))))
+        return out
+
+    def grid(self):
+        y = np.empty(self.params.NY)
+        self._chk(self.L.owt_get_grid(self.h, _L.dptr(y)))
+        return y
+
+    def enqueue_stage(self, stage):
+        """Enqueue one stage (0 modes, 1 mean, 2 transforms, 3 nonlinear) for timing."""
+        self._chk(self.L.owt_enqueue_stage(self.h, int(stage)))
+
+    def set_precision(self, precision):
+        self._chk(self.L.owt_set_precision(self.h, _L.PREC[precision]))
+
+    def use_graph(self, on=True):
+        self._chk(self.L.owt_use_graph(self.h, 1 if on else 0))
+
+    @property
+    def step(self):
+        v = C.c_int64()
+        self._chk(self.L.owt_get_step(self.h, C.byref(v)))
+        return v.value
+
+    @property
+    def launch_count(self):
+        v = C.c_int64()
+        self._chk(self.L.owt_get_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    @property
+    def stream(self):
+        v = C.c_void_p()
+        self._chk(self.L.owt_get_stream(self.h, C.byref(v)))
+        return v.value
