@@ -157,6 +157,21 @@ int owt_get_launch_count(const owt_handle *h, int64_t *count);
 int owt_get_grid(const owt_handle *h, double *y);
 int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
 
+/* Options and introspection (no counterpart in the reference).
+ * OWT_OPT_FORCE_DENSE_BANDS: 1 = sweep the full band of the v-system in every
+ *   column instead of skipping structurally-zero interior entries (the two
+ *   give the same result; this exists to test that).
+ * OWT_INFO_SPARSE_SOLVE: 1 if the interior-sparse v-system solve is active.
+ * OWT_INFO_PATTERN_VIOLATIONS: modes whose factors fell outside the sparse
+ *   pattern at setup (any such mode selects the full-band solve).
+ * OWT_INFO_DEVICE_BYTES: device memory held by the handle. */
+#define OWT_OPT_FORCE_DENSE_BANDS 1
+#define OWT_INFO_SPARSE_SOLVE 1
+#define OWT_INFO_PATTERN_VIOLATIONS 2
+#define OWT_INFO_DEVICE_BYTES 3
+int owt_set_option(owt_handle *h, int option, int64_t value);
+int owt_get_info(const owt_handle *h, int what, int64_t *value);
+
 /* Measurement aid, no counterpart in the reference: enqueue one stage of the
  * step on the handle's stream without advancing the step counter, so a caller
  * can time it with CUDA events on that stream.  The stage overwrites the

@@ -35,10 +35,13 @@ void ck(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+thread_local size_t *g_alloc_counter = nullptr;
+
 template <typename T>
 T *dalloc(size_t n, std::vector<void *> &owned) {
   void *p = nullptr;
   if (n == 0) n = 1;
+  if (g_alloc_counter) *g_alloc_counter += n * sizeof(T);
   cudaError_t e = cudaMalloc(&p, n * sizeof(T));
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -59,6 +62,7 @@ T *upload(const std::vector<T> &v, std::vector<void *> &owned, cudaStream_t st) 
 struct BandDev {
   double *ab = nullptr;
   uint8_t *piv = nullptr;
+  double *rscale = nullptr;  // inverse row scales [n][U] (null: rows not scaled)
   int n = 0, kl = 0, ku = 0;
 };
 
@@ -78,6 +82,8 @@ struct owt_handle {
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   bool q_dirty[3] = {false, false, false};
+  bool sparse_v = false;        // interior fill of every v-system inside the masks
+  int pattern_violations = 0;   // modes that forced the dense solve
   Grid grid;
   double Ly = 0, inv_cg0 = 0;
   size_t fs = 0;  // complex values per spectral field
@@ -120,7 +126,10 @@ struct owt_handle {
   }
 
   // ---- setup -----------------------------------------------------------------
+  size_t device_bytes = 0;
   void setup(const owt_params &prm) {
+    g_alloc_counter = &device_bytes;
+    struct Reset { ~Reset() { g_alloc_counter = nullptr; } } reset_counter;
     p = prm;
     NX = (int)p.NX; NY = (int)p.NY; NZ = (int)p.NZ;
     if (p.NX < 4 || p.NZ < 4 || p.NX % 2 || p.NZ % 2)
@@ -138,6 +147,8 @@ struct owt_handle {
     std::vector<int> rx, rz;
     if (!fft_radices(NX2, rx) || !fft_radices(NZ2, rz))
       throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must be of the form 2^a 3^b");
+    if (NX2 > 1024 || NZ2 > 1024)
+      throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must not exceed 1024 (one thread per point of a line)");
     px.L = NX2; px.nst = (int)rx.size();
     for (size_t q = 0; q < rx.size(); ++q) px.R[q] = rx[q];
     pz.L = NZ2; pz.nst = (int)rz.size();
@@ -192,26 +203,40 @@ struct owt_handle {
 
     // band factorizations
     double *d_sa = upload(sa, owned, st), *d_sb = upload(sb, owned, st), *d_icg = inv_cg;
-    auto factor = [&](BandDev &bd, const BandTemplate &t, int U, const double *s1, const double *s2) {
+    auto factor = [&](BandDev &bd, const BandTemplate &t, int U, const double *s1, const double *s2, bool rows) {
       bd.n = t.n; bd.kl = t.kl; bd.ku = t.ku;
       const size_t nb = 2 * (size_t)t.kl + t.ku + 1;
       bd.ab = dalloc<double>(nb * t.n * (size_t)U, owned);
       bd.piv = dalloc<uint8_t>((size_t)t.n * U, owned);
+      if (rows) bd.rscale = dalloc<double>((size_t)t.n * U, owned);
       std::vector<void *> tmp;
       double *d0 = upload(t.t0, tmp, st), *d1 = upload(t.t1, tmp, st), *d2 = upload(t.t2, tmp, st);
-      launch_band_factor(t.kl, t.ku, bd.ab, bd.piv, t.n, U, d0, d1, d2, s1, s2, d_err, st);
+      launch_band_factor(t.kl, t.ku, bd.ab, bd.piv, t.n, U, d0, d1, d2, s1, s2, bd.rscale, d_err, st);
       ++launches;
       check_launch("band factorization");
       ck(cudaStreamSynchronize(st), "band factorization");
       for (void *q : tmp) cudaFree(q);
     };
-    factor(bv, tv, Uq, d_sa, d_sb);
-    factor(bg, tg, Uq, d_icg, nullptr);
-    factor(b1, t1, 1, nullptr, nullptr);
-    factor(b2, t2, 1, nullptr, nullptr);
+    factor(bv, tv, Uq, d_sa, d_sb, true);
+    factor(bg, tg, Uq, d_icg, nullptr, true);
+    factor(b1, t1, 1, nullptr, nullptr, false);
+    factor(b2, t2, 1, nullptr, nullptr, false);
     int herr = 0;
     ck(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost), "factor status");
     if (herr) throw OwtError(OWT_ERR_NUMERIC, "LU factorization failed. Matrix A may be singular.");
+    // interior fill inside the compile-time masks? then the sparse solve applies
+    sparse_v = false;
+    if (bv.n % 5 == 0 && bv.n > 2 * 140) {
+      int *d_bad = dalloc<int>(1, owned);
+      ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset");
+      launch_check_pattern(bv.ab, bv.n, Uq, d_bad, st);
+      ++launches;
+      int nbad = 0;
+      ck(cudaMemcpyAsync(&nbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st), "pattern check");
+      ck(cudaStreamSynchronize(st), "pattern check");
+      sparse_v = (nbad == 0);
+      pattern_violations = nbad;
+    }
     rhs_node_v = upload(tv.rhs_node, owned, st);
     rb_col = upload(tg.rb_col, owned, st);
     rb_val = upload(tg.rb_val, owned, st);
@@ -338,9 +363,11 @@ struct owt_handle {
     a.ab_v = bv.ab; a.piv_v = bv.piv; a.n_v = bv.n;
     a.ab_g = bg.ab; a.piv_g = bg.piv; a.n_g = bg.n;
     a.rhs_node_v = rhs_node_v; a.rb_col = rb_col; a.rb_val = rb_val; a.inv_cg = inv_cg;
+    a.rs_v = bv.rscale; a.rs_g = bg.rscale;
+    a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
     a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg;
     a.step = d_step;
-    launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, st);
+    launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense, st);
   }
   void stage_mean() {
     MeanArgs ma{};
@@ -348,6 +375,7 @@ struct owt_handle {
     ma.inv_dt = 1.0 / p.dt; ma.nu = p.nu; ma.Ly = Ly; ma.inv_cg0 = inv_cg0;
     ma.c11 = c11; ma.c21 = c21; ma.c22 = c22;
     ma.ab_g = bg.ab; ma.piv_g = bg.piv; ma.rb_col = rb_col; ma.rb_val = rb_val;
+    ma.rs_g = bg.rscale; ma.inv_h = 1.0 / grid.ds; ma.inv_h2 = 1.0 / (grid.ds * grid.ds);
     ma.U_ring = U_ring; ma.W_ring = W_ring; ma.lx_ring = lxm_ring; ma.lz_ring = lzm_ring;
     ma.fx_ring = fx_ring; ma.fz_ring = fz_ring;
     ma.u_field = u; ma.w_field = w; ma.ox_field = ox; ma.oz_field = oz;
@@ -382,6 +410,7 @@ struct owt_handle {
     check_launch("time step");
   }
   int64_t per_step_launches = 0;
+  bool force_dense = false;  // testing aid: always sweep the full band
 
   void drop_graph() {
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
@@ -716,6 +745,25 @@ int owt_get_grid(const owt_handle *h, double *y) {
   if (!h || !y) return OWT_ERR_INVALID;
   std::memcpy(y, h->grid.y.data(), h->grid.y.size() * sizeof(double));
   return OWT_OK;
+}
+
+int owt_set_option(owt_handle *h, int option, int64_t value) {
+  return guard(h, [&] {
+    if (option != OWT_OPT_FORCE_DENSE_BANDS) throw OwtError(OWT_ERR_INVALID, "unknown option");
+    ck(cudaStreamSynchronize(h->st), "set option");
+    h->drop_graph();
+    h->force_dense = value != 0;
+  });
+}
+
+int owt_get_info(const owt_handle *h, int what, int64_t *value) {
+  if (!h || !value) return OWT_ERR_INVALID;
+  switch (what) {
+    case OWT_INFO_SPARSE_SOLVE: *value = (h->sparse_v && !h->force_dense) ? 1 : 0; return OWT_OK;
+    case OWT_INFO_PATTERN_VIOLATIONS: *value = h->pattern_violations; return OWT_OK;
+    case OWT_INFO_DEVICE_BYTES: *value = (int64_t)h->device_bytes; return OWT_OK;
+    default: return OWT_ERR_INVALID;
+  }
 }
 
 int owt_enqueue_stage(owt_handle *h, int stage) {

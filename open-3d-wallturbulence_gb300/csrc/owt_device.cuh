@@ -56,57 +56,83 @@ __device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx
 }
 
 template <typename T, bool BACKWARD>
+__device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R, int j, int nr, int ns, int base,
+                                          cpx<T> w1, cpx<T> w2, cpx<T> w3, bool twid) {
+  if (R == 4) {
+    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
+    if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); }
+    const cpx<T> t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
+    const cpx<T> d = csub(x1, x3);
+    // t3 = d * (sign i): forward multiplies by -i, backward by +i
+    const cpx<T> t3 = BACKWARD ? mk<T>(-d.y, d.x) : mk<T>(d.y, -d.x);
+    dst[base] = cadd(t0, t2);
+    dst[base + ns] = cadd(t1, t3);
+    dst[base + 2 * ns] = csub(t0, t2);
+    dst[base + 3 * ns] = csub(t1, t3);
+  } else if (R == 2) {
+    cpx<T> x0 = src[j], x1 = src[j + nr];
+    if (twid) x1 = cmul(x1, w1);
+    dst[base] = cadd(x0, x1);
+    dst[base + ns] = csub(x0, x1);
+  } else {  // R == 3
+    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
+    if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); }
+    const T s60 = (T)0.86602540378443864676372317075294;
+    const cpx<T> t = cadd(x1, x2);
+    const cpx<T> d = csub(x1, x2);
+    const cpx<T> m = mk<T>(x0.x - (T)0.5 * t.x, x0.y - (T)0.5 * t.y);
+    // u = d * (sign i sin60)
+    const cpx<T> u = BACKWARD ? mk<T>(-s60 * d.y, s60 * d.x) : mk<T>(s60 * d.y, -s60 * d.x);
+    dst[base] = cadd(x0, t);
+    dst[base + ns] = cadd(m, u);
+    dst[base + 2 * ns] = csub(m, u);
+  }
+}
+
+// nlines lines of length p.L, line q at a + q * lstride; result in the
+// returned buffer (a or b).  Each thread owns one butterfly index j per stage
+// and applies it to every (blockDim / (L/R))-th line, so index arithmetic and
+// twiddle loads happen once per stage; a block of L threads keeps every thread
+// busy for radix 2, 3 and 4 when nlines is a multiple of 12.
+template <typename T, bool BACKWARD>
 __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, const FftPlan &p,
                              const cpx<T> *__restrict__ tw) {
   const int L = p.L;
+  const int tid = threadIdx.x, nt = blockDim.x;
   int ns = 1;
   for (int s = 0; s < p.nst; ++s) {
     const int R = p.R[s];
     const int nr = L / R;
     const int step = L / (ns * R);
-    const int total = nlines * nr;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-      const int line = idx / nr;
-      const int j = idx - line * nr;
-      const int k = j % ns;
-      const cpx<T> *src = a + line * lstride;
-      cpx<T> *dst = b + line * lstride;
-      const int base = (j - k) * R + k;
-      if (R == 4) {
-        cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
-        if (k != 0) {
-          x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
-          x2 = cmul(x2, twiddle<T, BACKWARD>(tw, 2 * k * step));
-          x3 = cmul(x3, twiddle<T, BACKWARD>(tw, 3 * k * step));
+    const int per = nt / nr;  // lines per pass
+    if (per > 0) {
+      if (tid < per * nr) {
+        const int j = tid % nr, lo = tid / nr;
+        const int k = j % ns;
+        const int base = (j - k) * R + k;
+        const bool twid = k != 0;
+        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1;
+        if (twid) {
+          w1 = twiddle<T, BACKWARD>(tw, k * step);
+          if (R >= 3) w2 = twiddle<T, BACKWARD>(tw, 2 * k * step);
+          if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
         }
-        const cpx<T> t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
-        cpx<T> d = csub(x1, x3);
-        // t3 = d * (sign i): forward multiplies by -i, backward by +i
-        const cpx<T> t3 = BACKWARD ? mk<T>(-d.y, d.x) : mk<T>(d.y, -d.x);
-        dst[base] = cadd(t0, t2);
-        dst[base + ns] = cadd(t1, t3);
-        dst[base + 2 * ns] = csub(t0, t2);
-        dst[base + 3 * ns] = csub(t1, t3);
-      } else if (R == 2) {
-        cpx<T> x0 = src[j], x1 = src[j + nr];
-        if (k != 0) x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
-        dst[base] = cadd(x0, x1);
-        dst[base + ns] = csub(x0, x1);
-      } else {  // R == 3
-        cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
-        if (k != 0) {
-          x1 = cmul(x1, twiddle<T, BACKWARD>(tw, k * step));
-          x2 = cmul(x2, twiddle<T, BACKWARD>(tw, 2 * k * step));
+        for (int line = lo; line < nlines; line += per)
+          butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, base, w1, w2, w3, twid);
+      }
+    } else {
+      for (int idx = tid; idx < nlines * nr; idx += nt) {
+        const int line = idx / nr, j = idx - line * nr;
+        const int k = j % ns;
+        const bool twid = k != 0;
+        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1;
+        if (twid) {
+          w1 = twiddle<T, BACKWARD>(tw, k * step);
+          if (R >= 3) w2 = twiddle<T, BACKWARD>(tw, 2 * k * step);
+          if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
         }
-        const T s60 = (T)0.86602540378443864676372317075294;
-        const cpx<T> t = cadd(x1, x2);
-        const cpx<T> d = csub(x1, x2);
-        const cpx<T> m = mk<T>(x0.x - (T)0.5 * t.x, x0.y - (T)0.5 * t.y);
-        // u = d * (sign i sin60)
-        const cpx<T> u = BACKWARD ? mk<T>(-s60 * d.y, s60 * d.x) : mk<T>(s60 * d.y, -s60 * d.x);
-        dst[base] = cadd(x0, t);
-        dst[base + ns] = cadd(m, u);
-        dst[base + 2 * ns] = csub(m, u);
+        butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, (j - k) * R + k, w1, w2, w3,
+                               twid);
       }
     }
     __syncthreads();
@@ -191,6 +217,120 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
             const double uu = col[(size_t)(KV - t) * sn];
             w[(s + t) % WB].x -= uu * x.x;
             w[(s + t) % WB].y -= uu * x.y;
+          }
+          w[s] = (j - WB >= 0) ? yload(j - WB) : make_double2(0.0, 0.0);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same solve for the v-system, skipping the entries of L and U that are
+// structurally zero in interior columns.  Unknowns are interleaved by node
+// (column c is unknown type c mod 5 of node c / 5); after partial pivoting the
+// nonzero offsets of an interior column depend only on its type.  The masks
+// below are the union over wavenumbers, grid sizes and stretchings observed
+// when the factorization layout was designed; every factorization is checked
+// against them (k_check_pattern) and the dense solve is used if any mode
+// falls outside.  Columns within VB_EDGE of either end are always swept with
+// the full band.  Register rings are padded to multiples of 5 (20, 35) so that
+// the unknown type of every unrolled step is a compile-time constant.
+// ---------------------------------------------------------------------------
+constexpr int VB_EDGE = 60;
+// bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward);
+// argument: unknown type of column c
+__host__ __device__ constexpr unsigned vmask_l(int ty) {
+  return ty == 0 ? 0x77bfeu : ty == 1 ? 0x7bdfeu : ty == 2 ? 0x3defeu : ty == 3 ? 0x5ef7eu : 0x6f7beu;
+}
+__host__ __device__ constexpr unsigned long long vmask_u(int ty) {
+  return ty == 0 ? 0x3fffffeull : (ty == 1 || ty == 2) ? 0x7feull : 0xffffeull;
+}
+
+template <class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                    int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                    Out out) {
+  constexpr int KL = 18, KU = 15, KV = KL + KU;
+  constexpr int W = 20;    // >= KL + 1, multiple of 5
+  constexpr int WB = 35;   // >= KV + 1, multiple of 5
+  const size_t sn = (size_t)n * U;
+  {
+    double2 w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : make_double2(0.0, 0.0);
+    for (int j0 = 0; j0 < n; j0 += W) {
+      const bool sparse = (j0 >= VB_EDGE) && (j0 + W - 1 < n - VB_EDGE);
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int j = j0 + s;
+        if (j < n) {
+          const int off = piv[(size_t)j * U + u];
+#pragma unroll
+          for (int t = 1; t <= KL; ++t) {
+            if (off == t) {
+              const double2 tmp = w[s];
+              w[s] = w[(s + t) % W];
+              w[(s + t) % W] = tmp;
+            }
+          }
+          const double2 yj = w[s];
+          ystore(j, yj);
+          const double *col = ab + (size_t)j * U + u;
+          if (sparse) {
+#pragma unroll
+            for (int t = 1; t <= KL; ++t) {
+              if ((vmask_l(s % 5) >> t) & 1u) {
+                const double l = col[(size_t)(KV + t) * sn];
+                w[(s + t) % W].x -= l * yj.x;
+                w[(s + t) % W].y -= l * yj.y;
+              }
+            }
+          } else {
+#pragma unroll
+            for (int t = 1; t <= KL; ++t) {
+              const double l = col[(size_t)(KV + t) * sn];
+              w[(s + t) % W].x -= l * yj.x;
+              w[(s + t) % W].y -= l * yj.y;
+            }
+          }
+          w[s] = (j + W < n) ? rhs(j + W) : make_double2(0.0, 0.0);
+        }
+      }
+    }
+  }
+  {
+    double2 w[WB];
+#pragma unroll
+    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : make_double2(0.0, 0.0);
+    for (int jj = 0; jj < n; jj += WB) {
+      // columns n-1-jj .. n-1-jj-(WB-1); n is a multiple of 5, so the type of
+      // column n-1-jj-s is (4 - s) mod 5
+      const bool sparse = (n - 1 - jj < n - VB_EDGE) && (n - 1 - jj - (WB - 1) >= VB_EDGE);
+#pragma unroll
+      for (int s = 0; s < WB; ++s) {
+        const int j = n - 1 - (jj + s);
+        if (j >= 0) {
+          const double *col = ab + (size_t)j * U + u;
+          const double rinv = col[(size_t)KV * sn];
+          const double2 x = make_double2(w[s].x * rinv, w[s].y * rinv);
+          out(j, x);
+          if (sparse) {
+#pragma unroll
+            for (int t = 1; t <= KV; ++t) {
+              if ((vmask_u((4 - s % 5 + 5) % 5) >> t) & 1ull) {
+                const double uu = col[(size_t)(KV - t) * sn];
+                w[(s + t) % WB].x -= uu * x.x;
+                w[(s + t) % WB].y -= uu * x.y;
+              }
+            }
+          } else {
+#pragma unroll
+            for (int t = 1; t <= KV; ++t) {
+              const double uu = col[(size_t)(KV - t) * sn];
+              w[(s + t) % WB].x -= uu * x.x;
+              w[(s + t) % WB].y -= uu * x.y;
+            }
           }
           w[s] = (j - WB >= 0) ? yload(j - WB) : make_double2(0.0, 0.0);
         }

@@ -212,6 +212,20 @@ BandTemplate to_band(std::vector<Eq> &eqs, int n, int per_node) {
 
 }  // namespace
 
+// Column scaling: the unknown of type t >= 1 (a t-th compact derivative) is
+// solved for as h^t d_t, so that every unknown has the magnitude of v.
+static void scale_columns(BandTemplate &bt, const std::vector<double> &per_type) {
+  const int nb = bt.kl + bt.ku + 1;
+  for (int b = 0; b < nb; ++b)
+    for (int c = 0; c < bt.n; ++c) {
+      const double f = per_type[c % bt.per_node];
+      const size_t at = (size_t)b * bt.n + c;
+      bt.t0[at] *= f;
+      bt.t1[at] *= f;
+      bt.t2[at] *= f;
+    }
+}
+
 BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu) {
   const int N = g.N, T = 5;
   std::vector<Eq> eqs;
@@ -246,7 +260,10 @@ BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu) {
       }
       eqs.push_back(e);
     }
-  return to_band(eqs, T * N, T);
+  BandTemplate bt = to_band(eqs, T * N, T);
+  const double h = g.ds;
+  scale_columns(bt, {1.0, 1.0 / h, 1.0 / (h * h), 1.0 / (h * h * h), 1.0 / (h * h * h * h)});
+  return bt;
 }
 
 BandTemplate build_g_system(const Grid &g, const Stencils &st, double nu) {
@@ -269,6 +286,7 @@ BandTemplate build_g_system(const Grid &g, const Stencils &st, double nu) {
       eqs.push_back(e);
     }
   BandTemplate bt = to_band(eqs, T * N, T);
+  scale_columns(bt, {1.0 / g.ds, 1.0 / (g.ds * g.ds)});
   // rhs tables: row p = (1/cg) * sum over interior c of B_m[j][c] r_c
   for (int p = 0; p < bt.n; ++p) {
     const int m = bt.rb_col[(size_t)p * 5], j = bt.rb_col[(size_t)p * 5 + 1];

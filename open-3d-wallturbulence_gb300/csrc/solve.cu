@@ -29,7 +29,7 @@ template <int KL, int KU>
 __global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv, int n, int U,
                               const double *__restrict__ t0, const double *__restrict__ t1,
                               const double *__restrict__ t2, const double *__restrict__ s1,
-                              const double *__restrict__ s2, int *__restrict__ info) {
+                              const double *__restrict__ s2, double *__restrict__ rscale, int *__restrict__ info) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= U) return;
   constexpr int KV = KL + KU;
@@ -46,6 +46,17 @@ __global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv
       }
       AB(b, c) = v;
     }
+  // row equilibration: row p holds A(p, c) at band row KV + p - c
+  if (rscale) {
+    for (int p = 0; p < n; ++p) {
+      const int c0 = max(0, p - KL), c1 = min(n - 1, p + KU);
+      double mx = 0.0;
+      for (int c = c0; c <= c1; ++c) mx = fmax(mx, fabs(AB(KV + p - c, c)));
+      const double inv = mx > 0.0 ? 1.0 / mx : 1.0;
+      for (int c = c0; c <= c1; ++c) AB(KV + p - c, c) *= inv;
+      rscale[(size_t)p * U + u] = inv;
+    }
+  }
   int ju = 0;
   for (int j = 0; j < n; ++j) {
     const int km = min(KL, n - 1 - j);
@@ -79,12 +90,15 @@ __global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv
 }
 
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0,
-                        const double *t1, const double *t2, const double *s1, const double *s2, int *info,
-                        cudaStream_t st) {
+                        const double *t1, const double *t2, const double *s1, const double *s2, double *rscale,
+                        int *info, cudaStream_t st) {
   const int bs = 64, gs = (U + bs - 1) / bs;
-  if (kl == 18 && ku == 15) k_band_factor<18, 15><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
-  else if (kl == 6 && ku == 6) k_band_factor<6, 6><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
-  else if (kl == 2 && ku == 2) k_band_factor<2, 2><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, info);
+  if (kl == 18 && ku == 15)
+    k_band_factor<18, 15><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
+  else if (kl == 6 && ku == 6)
+    k_band_factor<6, 6><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
+  else if (kl == 2 && ku == 2)
+    k_band_factor<2, 2><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
 }
 
 bool band_supported(int kl, int ku) {
@@ -100,7 +114,7 @@ bool band_supported(int kl, int ku) {
 //  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
 // ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG>
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE>
 __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= a.M) return;
@@ -156,15 +170,17 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
         acc.x += b * r.x;
         acc.y += b * r.y;
       }
-      return make_double2(acc.x * icg, acc.y * icg);
+      const double sc = icg * a.rs_g[(size_t)p * a.U + u];
+      return make_double2(acc.x * sc, acc.y * sc);
     };
     auto ys = [&](int p, double2 y) { a.yg[(size_t)p * M + m] = y; };
     auto yl = [&](int p) -> double2 { return a.yg[(size_t)p * M + m]; };
     auto out = [&](int c, double2 x) {
       const int jn = c >> 1;
       if (c & 1) {
-        d2 = x;
+        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
       } else {
+        x = make_double2(x.x * a.inv_h, x.y * a.inv_h);
         const size_t at = (size_t)jn * M + m;
         double2 g = make_double2(0.0, 0.0);
         if (jn != 0 && jn != NY - 1) {
@@ -197,9 +213,10 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
       const double2 z0 = q0[at], z1 = q1[at], z2 = q2[at];
       const double vsx = x0.x * al0 + x1.x * al1 + x2.x * al2, vsy = x0.y * al0 + x1.y * al1 + x2.y * al2;
       const double qsx = z0.x * al0 + z1.x * al1 + z2.x * al2, qsy = z0.y * al0 + z1.y * al1 + z2.y * al2;
+      const double sc = a.rs_v[(size_t)p * a.U + u];
       double2 r;
-      r.x = (h0.x * be0 + h1.x * be1 + h2.x * be2) - k2dt * vsx + qsx * idt;
-      r.y = (h0.y * be0 + h1.y * be1 + h2.y * be2) - k2dt * vsy + qsy * idt;
+      r.x = ((h0.x * be0 + h1.x * be1 + h2.x * be2) - k2dt * vsx + qsx * idt) * sc;
+      r.y = ((h0.y * be0 + h1.y * be1 + h2.y * be2) - k2dt * vsy + qsy * idt) * sc;
       return r;
     };
     auto ys = [&](int p, double2 y) { a.yv[(size_t)p * M + m] = y; };
@@ -207,9 +224,9 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
     auto out = [&](int c, double2 x) {
       const int jn = c / 5, t = c - 5 * jn;
       if (t == 2) {
-        d2 = x;
+        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
       } else if (t == 1) {
-        d1 = x;
+        d1 = make_double2(x.x * a.inv_h, x.y * a.inv_h);
       } else if (t == 0) {
         const size_t at = (size_t)jn * M + m;
         vn[at] = x;
@@ -233,13 +250,41 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
         }
       }
     };
-    band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    if (SPARSE) band_solve_v_sparse(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    else band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
   }
 }
 
-void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, cudaStream_t st) {
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st) {
   const int bs = 128, gs = (a.M + bs - 1) / bs;
-  if (klv == 18 && kuv == 15 && klg == 6 && kug == 6) k_modes<18, 15, 6, 6><<<gs, bs, 0, st>>>(a);
+  if (klv == 18 && kuv == 15 && klg == 6 && kug == 6) {
+    if (sparse) k_modes<18, 15, 6, 6, true><<<gs, bs, 0, st>>>(a);
+    else k_modes<18, 15, 6, 6, false><<<gs, bs, 0, st>>>(a);
+  }
+}
+
+// Every factored v-system must keep its interior fill inside the masks: count
+// the modes whose L or U has a nonzero outside the masks in columns
+// [VB_EDGE, n - VB_EDGE).
+__global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int *__restrict__ bad) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= U) return;
+  constexpr int KL = 18, KU = 15, KV = KL + KU;
+  const size_t sn = (size_t)n * U;
+  int nbad = 0;
+  for (int c = VB_EDGE; c < n - VB_EDGE; ++c) {
+    const int ty = c % 5;
+    const double *col = ab + (size_t)c * U + u;
+    for (int t = 1; t <= KL; ++t)
+      if (!((vmask_l(ty) >> t) & 1u) && col[(size_t)(KV + t) * sn] != 0.0) ++nbad;
+    for (int t = 1; t <= KV; ++t)
+      if (!((vmask_u(ty) >> t) & 1ull) && col[(size_t)(KV - t) * sn] != 0.0) ++nbad;
+  }
+  if (nbad) atomicAdd(bad, 1);
+}
+
+void launch_check_pattern(const double *ab, int n, int U, int *bad, cudaStream_t st) {
+  k_check_pattern<<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
 }
 
 __global__ void k_advance(long long *step) { *step += 1; }
@@ -288,15 +333,17 @@ __global__ void k_mean(MeanArgs a) {
         acc.x += b * r.x;
         acc.y += b * r.y;
       }
-      return make_double2(acc.x * icg, acc.y * icg);
+      const double sc = icg * a.rs_g[(size_t)p * a.U];
+      return make_double2(acc.x * sc, acc.y * sc);
     };
     auto ys = [&](int p, double2 y) { yy[p] = y; };
     auto yl = [&](int p) -> double2 { return yy[p]; };
     auto out = [&](int c, double2 x) {
       const int jn = c >> 1;
       if (c & 1) {
-        d2 = x;
+        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
       } else {
+        x = make_double2(x.x * a.inv_h, x.y * a.inv_h);
         double2 g = make_double2(0.0, 0.0);
         if (jn != 0 && jn != NY - 1) {
           const double2 r = sg[jn];

@@ -19,6 +19,8 @@ struct ModeArgs {
   const int *rhs_node_v;
   const int *rb_col; const double *rb_val;
   const double *inv_cg;
+  const double *rs_v, *rs_g;  // inverse row scales [n][U]
+  double inv_h, inv_h2;       // unscaling of solved h d1, h^2 d2
   double2 *sg, *dg, *yv, *yg;  // scratch
   const long long *step;
 };
@@ -29,6 +31,8 @@ struct MeanArgs {
   const double *c11, *c21, *c22;
   const double *ab_g; const uint8_t *piv_g;
   const int *rb_col; const double *rb_val;
+  const double *rs_g;
+  double inv_h, inv_h2;
   double2 *U_ring, *W_ring, *lx_ring, *lz_ring;  // [3][NY]
   double *fx_ring, *fz_ring;                     // [3]
   double2 *u_field, *w_field, *ox_field, *oz_field;
@@ -89,8 +93,10 @@ struct XformArgs {
 
 bool band_supported(int kl, int ku);
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0, const double *t1,
-                        const double *t2, const double *s1, const double *s2, int *info, cudaStream_t st);
-void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, cudaStream_t st);
+                        const double *t2, const double *s1, const double *s2, double *rscale, int *info,
+                        cudaStream_t st);
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st);
+void launch_check_pattern(const double *ab, int n, int U, int *bad, cudaStream_t st);
 void launch_advance(long long *step, cudaStream_t st);
 void launch_mean(const MeanArgs &a, cudaStream_t st);
 void launch_nl(const NLArgs &a, cudaStream_t st);

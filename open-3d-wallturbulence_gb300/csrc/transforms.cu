@@ -27,14 +27,16 @@
 namespace owt {
 
 template <typename T> struct XCfg;
-template <> struct XCfg<double> { static constexpr int TX = 4; static constexpr int P = 2; };
-template <> struct XCfg<float> { static constexpr int TX = 8; static constexpr int P = 4; };
+// TX lines per z block, P (y, z) lines per x block (3P FFT lines).  Blocks
+// have as many threads as the line length (NZ2 or NX2, at most 1024).
+template <> struct XCfg<double> { static constexpr int TX = 6; static constexpr int P = 2; };
+template <> struct XCfg<float> { static constexpr int TX = 12; static constexpr int P = 4; };
 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_zback(XformArgs a) {
+__global__ void __launch_bounds__(1024) k_zback(XformArgs a) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(256) k_zback(XformArgs a) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_xlamb(XformArgs a) {
+__global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   constexpr int P = XCfg<T>::P;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(256) k_xlamb(XformArgs a) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_zfwd(XformArgs a) {
+__global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -178,11 +180,11 @@ static int lamb_t(const XformArgs &a, cudaStream_t st) {
   constexpr int TX = XCfg<T>::TX, P = XCfg<T>::P;
   const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
   dim3 gz((d.NXH + TX - 1) / TX, d.NY, 6);
-  k_zback<T><<<gz, 256, sz, st>>>(a);
+  k_zback<T><<<gz, d.NZ2, sz, st>>>(a);
   const size_t nl = (size_t)d.NY * d.NZ2;
-  k_xlamb<T><<<(unsigned)((nl + P - 1) / P), 256, sx, st>>>(a);
+  k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
   dim3 gf((d.NXH + TX - 1) / TX, d.NY, 3);
-  k_zfwd<T><<<gf, 256, sz, st>>>(a);
+  k_zfwd<T><<<gf, d.NZ2, sz, st>>>(a);
   return 3;
 }
 

