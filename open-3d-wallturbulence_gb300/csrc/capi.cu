@@ -282,6 +282,7 @@ struct owt_handle {
     mean_dy1 = dalloc<double2>(2 * (size_t)NY, owned);
     XformDims xd{NY, NZ, NXH, NZH, NX2, NZ2};
     ck(lamb_prepare(xd), "transform kernel attributes");
+    mean_smem = mean_prepare(NY, bg.n);
     zbuf = dalloc<unsigned char>(lamb_zbuf_bytes(xd, 0), owned);
     lbuf = dalloc<unsigned char>(lamb_lbuf_bytes(xd, 0), owned);
     for (int prec = 0; prec < 2; ++prec) {
@@ -322,6 +323,7 @@ struct owt_handle {
     a.ring_mask = (1 << 1) | (1 << 4);
     a.fs = fs;
     a.step = d_step;
+    a.mean_split = precision == OWT_PREC_MIXED ? 1 : 0;
     a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
     a.zbuf = zbuf; a.lbuf = lbuf;
     a.px = px; a.pz = pz;
@@ -380,7 +382,7 @@ struct owt_handle {
     ma.fx_ring = fx_ring; ma.fz_ring = fz_ring;
     ma.u_field = u; ma.w_field = w; ma.ox_field = ox; ma.oz_field = oz;
     ma.scratch = mean_scratch; ma.dy1 = mean_dy1; ma.step = d_step; ma.err = d_err;
-    launch_mean(ma, st);
+    launch_mean(ma, mean_smem, st);
   }
 
   void run_steps(int64_t n) {
@@ -411,6 +413,7 @@ struct owt_handle {
   }
   int64_t per_step_launches = 0;
   bool force_dense = false;  // testing aid: always sweep the full band
+  bool mean_smem = false;    // staged mean-mode solve in shared memory
 
   void drop_graph() {
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }

@@ -142,6 +142,16 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
   return a;
 }
 
+// Value helpers so the band solves run on one real component (double) or a
+// complex value (double2) per thread.
+__device__ __forceinline__ void fms(double &w, double l, double y) { w -= l * y; }
+__device__ __forceinline__ void fms(double2 &w, double l, double2 y) { w.x -= l * y.x; w.y -= l * y.y; }
+__device__ __forceinline__ double scal(double w, double r) { return w * r; }
+__device__ __forceinline__ double2 scal(double2 w, double r) { return make_double2(w.x * r, w.y * r); }
+template <class V> __device__ __forceinline__ V vzero();
+template <> __device__ __forceinline__ double vzero<double>() { return 0.0; }
+template <> __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
+
 // ---------------------------------------------------------------------------
 // Banded LU solve, the algorithm of LAPACK dgbtrs ('N') on factors produced by
 // the dgbtf2 algorithm (see k_band_factor): forward sweep applying the row
@@ -163,13 +173,14 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
 template <int KL, int KU, class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
                                            int U, int u, Rhs rhs, YStore ystore, YLoad yload, Out out) {
+  using V = decltype(rhs(0));
   constexpr int KV = KL + KU;
   constexpr int W = KL + 1;
   const size_t sn = (size_t)n * U;  // stride between band rows
   {
-    double2 w[W];
+    V w[W];
 #pragma unroll
-    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : make_double2(0.0, 0.0);
+    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : vzero<V>();
     for (int j0 = 0; j0 < n; j0 += W) {
 #pragma unroll
       for (int s = 0; s < W; ++s) {
@@ -179,46 +190,37 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 #pragma unroll
           for (int t = 1; t < W; ++t) {
             if (off == t) {
-              const double2 tmp = w[s];
+              const V tmp = w[s];
               w[s] = w[(s + t) % W];
               w[(s + t) % W] = tmp;
             }
           }
-          const double2 yj = w[s];
+          const V yj = w[s];
           ystore(j, yj);
           const double *col = ab + (size_t)j * U + u;
 #pragma unroll
-          for (int t = 1; t < W; ++t) {
-            const double l = col[(size_t)(KV + t) * sn];
-            w[(s + t) % W].x -= l * yj.x;
-            w[(s + t) % W].y -= l * yj.y;
-          }
-          w[s] = (j + W < n) ? rhs(j + W) : make_double2(0.0, 0.0);
+          for (int t = 1; t < W; ++t) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
+          w[s] = (j + W < n) ? rhs(j + W) : vzero<V>();
         }
       }
     }
   }
   {
     constexpr int WB = KV + 1;
-    double2 w[WB];
+    V w[WB];
 #pragma unroll
-    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : make_double2(0.0, 0.0);
+    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : vzero<V>();
     for (int jj = 0; jj < n; jj += WB) {
 #pragma unroll
       for (int s = 0; s < WB; ++s) {
         const int j = n - 1 - (jj + s);
         if (j >= 0) {
           const double *col = ab + (size_t)j * U + u;
-          const double rinv = col[(size_t)KV * sn];
-          const double2 x = make_double2(w[s].x * rinv, w[s].y * rinv);
+          const V x = scal(w[s], col[(size_t)KV * sn]);
           out(j, x);
 #pragma unroll
-          for (int t = 1; t < WB; ++t) {
-            const double uu = col[(size_t)(KV - t) * sn];
-            w[(s + t) % WB].x -= uu * x.x;
-            w[(s + t) % WB].y -= uu * x.y;
-          }
-          w[s] = (j - WB >= 0) ? yload(j - WB) : make_double2(0.0, 0.0);
+          for (int t = 1; t < WB; ++t) fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
+          w[s] = (j - WB >= 0) ? yload(j - WB) : vzero<V>();
         }
       }
     }
@@ -240,25 +242,27 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 constexpr int VB_EDGE = 60;
 // bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward);
 // argument: unknown type of column c
+// (masks of the equilibrated systems: 31.2 entries per column instead of 51)
 __host__ __device__ constexpr unsigned vmask_l(int ty) {
-  return ty == 0 ? 0x77bfeu : ty == 1 ? 0x7bdfeu : ty == 2 ? 0x3defeu : ty == 3 ? 0x5ef7eu : 0x6f7beu;
+  return ty == 0 ? 0x5fffeu : ty == 1 ? 0x6fffeu : ty == 2 ? 0x77ffeu : ty == 3 ? 0x7bffeu : 0x3dffeu;
 }
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
-  return ty == 0 ? 0x3fffffeull : (ty == 1 || ty == 2) ? 0x7feull : 0xffffeull;
+  return ty <= 2 ? 0x1fffeull : ty == 3 ? 0x7ffeull : 0x7feull;
 }
 
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
+  using V = decltype(rhs(0));
   constexpr int KL = 18, KU = 15, KV = KL + KU;
   constexpr int W = 20;    // >= KL + 1, multiple of 5
   constexpr int WB = 35;   // >= KV + 1, multiple of 5
   const size_t sn = (size_t)n * U;
   {
-    double2 w[W];
+    V w[W];
 #pragma unroll
-    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : make_double2(0.0, 0.0);
+    for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : vzero<V>();
     for (int j0 = 0; j0 < n; j0 += W) {
       const bool sparse = (j0 >= VB_EDGE) && (j0 + W - 1 < n - VB_EDGE);
 #pragma unroll
@@ -269,40 +273,31 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
 #pragma unroll
           for (int t = 1; t <= KL; ++t) {
             if (off == t) {
-              const double2 tmp = w[s];
+              const V tmp = w[s];
               w[s] = w[(s + t) % W];
               w[(s + t) % W] = tmp;
             }
           }
-          const double2 yj = w[s];
+          const V yj = w[s];
           ystore(j, yj);
           const double *col = ab + (size_t)j * U + u;
           if (sparse) {
 #pragma unroll
-            for (int t = 1; t <= KL; ++t) {
-              if ((vmask_l(s % 5) >> t) & 1u) {
-                const double l = col[(size_t)(KV + t) * sn];
-                w[(s + t) % W].x -= l * yj.x;
-                w[(s + t) % W].y -= l * yj.y;
-              }
-            }
+            for (int t = 1; t <= KL; ++t)
+              if ((vmask_l(s % 5) >> t) & 1u) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
           } else {
 #pragma unroll
-            for (int t = 1; t <= KL; ++t) {
-              const double l = col[(size_t)(KV + t) * sn];
-              w[(s + t) % W].x -= l * yj.x;
-              w[(s + t) % W].y -= l * yj.y;
-            }
+            for (int t = 1; t <= KL; ++t) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
           }
-          w[s] = (j + W < n) ? rhs(j + W) : make_double2(0.0, 0.0);
+          w[s] = (j + W < n) ? rhs(j + W) : vzero<V>();
         }
       }
     }
   }
   {
-    double2 w[WB];
+    V w[WB];
 #pragma unroll
-    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : make_double2(0.0, 0.0);
+    for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : vzero<V>();
     for (int jj = 0; jj < n; jj += WB) {
       // columns n-1-jj .. n-1-jj-(WB-1); n is a multiple of 5, so the type of
       // column n-1-jj-s is (4 - s) mod 5
@@ -312,27 +307,17 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
         const int j = n - 1 - (jj + s);
         if (j >= 0) {
           const double *col = ab + (size_t)j * U + u;
-          const double rinv = col[(size_t)KV * sn];
-          const double2 x = make_double2(w[s].x * rinv, w[s].y * rinv);
+          const V x = scal(w[s], col[(size_t)KV * sn]);
           out(j, x);
           if (sparse) {
 #pragma unroll
-            for (int t = 1; t <= KV; ++t) {
-              if ((vmask_u((4 - s % 5 + 5) % 5) >> t) & 1ull) {
-                const double uu = col[(size_t)(KV - t) * sn];
-                w[(s + t) % WB].x -= uu * x.x;
-                w[(s + t) % WB].y -= uu * x.y;
-              }
-            }
+            for (int t = 1; t <= KV; ++t)
+              if ((vmask_u((4 - s % 5 + 5) % 5) >> t) & 1ull) fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
           } else {
 #pragma unroll
-            for (int t = 1; t <= KV; ++t) {
-              const double uu = col[(size_t)(KV - t) * sn];
-              w[(s + t) % WB].x -= uu * x.x;
-              w[(s + t) % WB].y -= uu * x.y;
-            }
+            for (int t = 1; t <= KV; ++t) fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
           }
-          w[s] = (j - WB >= 0) ? yload(j - WB) : make_double2(0.0, 0.0);
+          w[s] = (j - WB >= 0) ? yload(j - WB) : vzero<V>();
         }
       }
     }

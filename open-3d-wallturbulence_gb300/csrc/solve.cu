@@ -106,7 +106,8 @@ bool band_supported(int kl, int ku) {
 }
 
 // ---------------------------------------------------------------------------
-// Mode kernel: one thread per Fourier mode.  For mode (kz, kx):
+// Mode kernel: two threads per Fourier mode (one per real component).  For
+// mode (kz, kx):
 //  1. source_g = sum beta Hg_l + sum alpha g_l / dt      (solver.cpp:573-574)
 //  2. omega_y-system: g and DY1 g                         (solver.cpp:578, 603)
 //  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
@@ -116,7 +117,10 @@ bool band_supported(int kl, int ku) {
 // ---------------------------------------------------------------------------
 template <int KLV, int KUV, int KLG, int KUG, bool SPARSE>
 __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  // Two threads per mode, one per real component (the band systems are real):
+  // lane 2m handles Re, lane 2m+1 Im; the pair's factor loads coincide.
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = tid >> 1, comp = tid & 1;
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
   const int k = m / a.NXH, i = m - k * a.NXH;
@@ -126,127 +130,118 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
   const double k2 = kx * kx + kz * kz;
   const long long s = *a.step;
   const int h = ring_head(s);
-  const size_t fs = (size_t)NY * M;
-  const double2 *v0 = a.v_ring + (size_t)h * fs, *v1 = a.v_ring + (size_t)((h + 1) % 3) * fs,
-                *v2 = a.v_ring + (size_t)((h + 2) % 3) * fs;
-  const double2 *g0 = a.g_ring + (size_t)h * fs, *g1 = a.g_ring + (size_t)((h + 1) % 3) * fs,
-                *g2 = a.g_ring + (size_t)((h + 2) % 3) * fs;
-  const double2 *hv0 = a.hv_ring + (size_t)h * fs, *hv1 = a.hv_ring + (size_t)((h + 1) % 3) * fs,
-                *hv2 = a.hv_ring + (size_t)((h + 2) % 3) * fs;
-  const double2 *hg0 = a.hg_ring + (size_t)h * fs, *hg1 = a.hg_ring + (size_t)((h + 1) % 3) * fs,
-                *hg2 = a.hg_ring + (size_t)((h + 2) % 3) * fs;
-  const double2 *q0 = a.q_ring + (size_t)h * fs, *q1 = a.q_ring + (size_t)((h + 1) % 3) * fs,
-                *q2 = a.q_ring + (size_t)((h + 2) % 3) * fs;
+  const size_t fs2 = 2 * (size_t)NY * M;  // doubles per field
+  auto lvl = [&](const double2 *ring, int l) {
+    return reinterpret_cast<const double *>(ring) + (size_t)((h + l) % 3) * fs2 + comp;
+  };
+  const double *v0 = lvl(a.v_ring, 0), *v1 = lvl(a.v_ring, 1), *v2 = lvl(a.v_ring, 2);
+  const double *g0 = lvl(a.g_ring, 0), *g1 = lvl(a.g_ring, 1), *g2 = lvl(a.g_ring, 2);
+  const double *hv0 = lvl(a.hv_ring, 0), *hv1 = lvl(a.hv_ring, 1), *hv2 = lvl(a.hv_ring, 2);
+  const double *hg0 = lvl(a.hg_ring, 0), *hg1 = lvl(a.hg_ring, 1), *hg2 = lvl(a.hg_ring, 2);
+  const double *q0 = lvl(a.q_ring, 0), *q1 = lvl(a.q_ring, 1), *q2 = lvl(a.q_ring, 2);
   const int hn = (h + 2) % 3;  // slot of the new level 0
-  double2 *vn = a.v_ring + (size_t)hn * fs;
-  double2 *gn = a.g_ring + (size_t)hn * fs;
-  double2 *qn = a.q_ring + (size_t)hn * fs;
+  double *vn = reinterpret_cast<double *>(a.v_ring) + (size_t)hn * fs2 + comp;
+  double *gn = reinterpret_cast<double *>(a.g_ring) + (size_t)hn * fs2 + comp;
+  double *qn = reinterpret_cast<double *>(a.q_ring) + (size_t)hn * fs2 + comp;
+  double *sg = reinterpret_cast<double *>(a.sg) + comp;
+  double *dg = reinterpret_cast<double *>(a.dg) + comp;
+  double *yv = reinterpret_cast<double *>(a.yv) + comp;
+  double *yg = reinterpret_cast<double *>(a.yg) + comp;
+  auto E = [&](int j) { return 2 * ((size_t)j * M + m); };  // offset of (j, m) in doubles
   const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
   const double idt = a.inv_dt;
 
-  // 1. source_g, walls zero (solver.cpp:598-599)
+  // 1. source_g, walls zero (solver.cpp:573-574, 598-599)
   for (int j = 0; j < NY; ++j) {
-    const size_t at = (size_t)j * M + m;
-    double2 r = make_double2(0.0, 0.0);
-    if (j != 0 && j != NY - 1) {
-      const double2 x0 = hg0[at], x1 = hg1[at], x2 = hg2[at];
-      const double2 y0 = g0[at], y1 = g1[at], y2 = g2[at];
-      r.x = (x0.x * be0 + x1.x * be1 + x2.x * be2) + (y0.x * al0 + y1.x * al1 + y2.x * al2) * idt;
-      r.y = (x0.y * be0 + x1.y * be1 + x2.y * be2) + (y0.y * al0 + y1.y * al1 + y2.y * al2) * idt;
-    }
-    a.sg[at] = r;
+    const size_t e = E(j);
+    double r = 0.0;
+    if (j != 0 && j != NY - 1)
+      r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
+    sg[e] = r;
   }
 
-  // 2. omega_y-system
+  // 2. omega_y-system: g and DY1 g
   const double icg = a.inv_cg[u];
   {
-    double2 d2 = make_double2(0.0, 0.0);
-    auto rhs = [&](int p) -> double2 {
-      double2 acc = make_double2(0.0, 0.0);
+    double d2 = 0.0;
+    auto rhs = [&](int p) -> double {
+      double acc = 0.0;
 #pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        const double b = a.rb_val[p * 5 + e];
-        const double2 r = a.sg[(size_t)a.rb_col[p * 5 + e] * M + m];
-        acc.x += b * r.x;
-        acc.y += b * r.y;
-      }
-      const double sc = icg * a.rs_g[(size_t)p * a.U + u];
-      return make_double2(acc.x * sc, acc.y * sc);
+      for (int q = 0; q < 5; ++q) acc += a.rb_val[p * 5 + q] * sg[E(a.rb_col[p * 5 + q])];
+      return acc * (icg * a.rs_g[(size_t)p * a.U + u]);
     };
-    auto ys = [&](int p, double2 y) { a.yg[(size_t)p * M + m] = y; };
-    auto yl = [&](int p) -> double2 { return a.yg[(size_t)p * M + m]; };
-    auto out = [&](int c, double2 x) {
+    auto ys = [&](int p, double y) { yg[E(p)] = y; };
+    auto yl = [&](int p) -> double { return yg[E(p)]; };
+    auto out = [&](int c, double x) {
       const int jn = c >> 1;
       if (c & 1) {
-        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
+        d2 = x * a.inv_h2;
       } else {
-        x = make_double2(x.x * a.inv_h, x.y * a.inv_h);
-        const size_t at = (size_t)jn * M + m;
-        double2 g = make_double2(0.0, 0.0);
-        if (jn != 0 && jn != NY - 1) {
-          const double2 r = a.sg[at];
-          const double w1 = a.nu * a.c21[jn], w2 = a.nu * a.c22[jn];
-          g.x = (r.x + w1 * x.x + w2 * d2.x) * icg;
-          g.y = (r.y + w1 * x.y + w2 * d2.y) * icg;
-        }
-        gn[at] = g;
-        const double c11 = a.c11[jn];
-        a.dg[at] = make_double2(c11 * x.x, c11 * x.y);
+        x *= a.inv_h;
+        const size_t e = E(jn);
+        double g = 0.0;
+        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nu * a.c21[jn] * x + a.nu * a.c22[jn] * d2) * icg;
+        gn[e] = g;
+        dg[e] = a.c11[jn] * x;
       }
     };
     band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
   }
+  __syncwarp(__activemask());  // the partner's g, DY1 g are read below
 
-  // 3-5. v-system and the horizontal components
+  // 3-5. v-system, then solve_horizontal's components
   {
     const double k2dt = k2 * idt;
     const bool horiz = !(k2 < 1.e-8);
     const double ik2 = horiz ? 1.0 / k2 : 0.0;
     const double ax = kx * ik2, az = kz * ik2;
-    double2 d1 = make_double2(0.0, 0.0), d2 = make_double2(0.0, 0.0);
-    auto rhs = [&](int p) -> double2 {
+    const double kzk2 = kz * k2, kxk2 = kx * k2;
+    double d1 = 0.0, d2 = 0.0;
+    auto rhs = [&](int p) -> double {
       const int j = a.rhs_node_v[p];
-      if (j < 0) return make_double2(0.0, 0.0);
-      const size_t at = (size_t)j * M + m;
-      const double2 h0 = hv0[at], h1 = hv1[at], h2 = hv2[at];
-      const double2 x0 = v0[at], x1 = v1[at], x2 = v2[at];
-      const double2 z0 = q0[at], z1 = q1[at], z2 = q2[at];
-      const double vsx = x0.x * al0 + x1.x * al1 + x2.x * al2, vsy = x0.y * al0 + x1.y * al1 + x2.y * al2;
-      const double qsx = z0.x * al0 + z1.x * al1 + z2.x * al2, qsy = z0.y * al0 + z1.y * al1 + z2.y * al2;
-      const double sc = a.rs_v[(size_t)p * a.U + u];
-      double2 r;
-      r.x = ((h0.x * be0 + h1.x * be1 + h2.x * be2) - k2dt * vsx + qsx * idt) * sc;
-      r.y = ((h0.y * be0 + h1.y * be1 + h2.y * be2) - k2dt * vsy + qsy * idt) * sc;
-      return r;
+      if (j < 0) return 0.0;
+      const size_t e = E(j);
+      const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
+      const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
+      const double r = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
+      return r * a.rs_v[(size_t)p * a.U + u];
     };
-    auto ys = [&](int p, double2 y) { a.yv[(size_t)p * M + m] = y; };
-    auto yl = [&](int p) -> double2 { return a.yv[(size_t)p * M + m]; };
-    auto out = [&](int c, double2 x) {
+    auto ys = [&](int p, double y) { yv[E(p)] = y; };
+    auto yl = [&](int p) -> double { return yv[E(p)]; };
+    auto out = [&](int c, double x) {
       const int jn = c / 5, t = c - 5 * jn;
       if (t == 2) {
-        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
+        d2 = x * a.inv_h2;
       } else if (t == 1) {
-        d1 = make_double2(x.x * a.inv_h, x.y * a.inv_h);
+        d1 = x * a.inv_h;
       } else if (t == 0) {
-        const size_t at = (size_t)jn * M + m;
-        vn[at] = x;
-        const double c21 = a.c21[jn], c22 = a.c22[jn], c11 = a.c11[jn];
-        const double2 q = make_double2(c21 * d1.x + c22 * d2.x, c21 * d1.y + c22 * d2.y);
-        qn[at] = q;
+        const size_t e = E(jn);
+        vn[e] = x;
+        const double q = a.c21[jn] * d1 + a.c22[jn] * d2;
+        qn[e] = q;
         if (horiz) {
-          const double2 dv = make_double2(c11 * d1.x, c11 * d1.y);
-          const double2 g = gn[at], dgv = a.dg[at];
+          const double dv = a.c11[jn] * d1;
+          const unsigned mask = __activemask();
+          const double xo = __shfl_xor_sync(mask, x, 1), dvo = __shfl_xor_sync(mask, dv, 1),
+                       qo = __shfl_xor_sync(mask, q, 1);
+          // full complex values (re, im) of v, DY1 v, DY2 v, g, DY1 g
+          const double vr = comp ? xo : x, vi = comp ? x : xo;
+          const double dvr = comp ? dvo : dv, dvi = comp ? dv : dvo;
+          const double qr = comp ? qo : q, qi = comp ? q : qo;
+          const double *gp = gn - comp, *dgp = dg - comp;
+          const double gr = gp[e], gi = gp[e + 1], dgr = dgp[e], dgi = dgp[e + 1];
           // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
-          const double2 uu = make_double2(-ax * dv.y + az * g.y, ax * dv.x - az * g.x);
-          const double2 ww = make_double2(-ax * g.y - az * dv.y, ax * g.x + az * dv.x);
           // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
-          const double kzk2 = kz * k2, kxk2 = kx * k2;
-          const double tx = kx * dgv.x + kz * q.x - kzk2 * x.x, ty = kx * dgv.y + kz * q.y - kzk2 * x.y;
-          const double sx = kz * dgv.x - kx * q.x + kxk2 * x.x, sy = kz * dgv.y - kx * q.y + kxk2 * x.y;
-          a.u_out[at] = uu;
-          a.w_out[at] = ww;
-          a.ox_out[at] = make_double2(-ty * ik2, tx * ik2);
-          a.oz_out[at] = make_double2(-sy * ik2, sx * ik2);
+          const double ur = -ax * dvi + az * gi, ui = ax * dvr - az * gr;
+          const double wr = -ax * gi - az * dvi, wi = ax * gr + az * dvr;
+          const double tx = kx * dgr + kz * qr - kzk2 * vr, ty = kx * dgi + kz * qi - kzk2 * vi;
+          const double sx = kz * dgr - kx * qr + kxk2 * vr, sy = kz * dgi - kx * qi + kxk2 * vi;
+          double *uo = reinterpret_cast<double *>(a.u_out), *wo = reinterpret_cast<double *>(a.w_out);
+          double *oxo = reinterpret_cast<double *>(a.ox_out), *ozo = reinterpret_cast<double *>(a.oz_out);
+          uo[e + comp] = comp ? ui : ur;
+          wo[e + comp] = comp ? wi : wr;
+          oxo[e + comp] = comp ? tx * ik2 : -ty * ik2;
+          ozo[e + comp] = comp ? sx * ik2 : -sy * ik2;
         }
       }
     };
@@ -256,7 +251,7 @@ __global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
 }
 
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st) {
-  const int bs = 128, gs = (a.M + bs - 1) / bs;
+  const int bs = 128, gs = (int)((2 * (long long)a.M + bs - 1) / bs);
   if (klv == 18 && kuv == 15 && klg == 6 && kug == 6) {
     if (sparse) k_modes<18, 15, 6, 6, true><<<gs, bs, 0, st>>>(a);
     else k_modes<18, 15, 6, 6, false><<<gs, bs, 0, st>>>(a);
@@ -297,17 +292,41 @@ void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>
 // velocity U, thread 1 for W, each with the omega_y-system of mode (0, 0)
 // (the same matrix as solve_mean's A).
 // ---------------------------------------------------------------------------
+template <bool SMEM>
 __global__ void k_mean(MeanArgs a) {
   const int t = threadIdx.x;
-  const int NY = a.NY;
+  const int NY = a.NY, n = a.n_g;
   const int h = ring_head(*a.step);
   const int o0 = (h + 1) % 3, o1 = (h + 2) % 3, o2 = h;
+  // The factors of mode (0, 0) are strided by the number of unique modes in
+  // global memory; a sequential solve on them is latency-bound, so the block
+  // first gathers them (and the scratch vectors) into shared memory.
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int NB = 2 * 6 + 6 + 1;
+  const double *ab = a.ab_g;
+  const uint8_t *piv = a.piv_g;
+  const double *rs = a.rs_g;
+  int stride = a.U;
+  double2 *scr = a.scratch;
+  if (SMEM) {
+    double2 *ssc = reinterpret_cast<double2 *>(smraw);             // 2 NY + 2 n
+    double *sab = reinterpret_cast<double *>(ssc + 2 * NY + 2 * n);  // NB n
+    double *srs = sab + (size_t)NB * n;                             // n
+    uint8_t *spv = reinterpret_cast<uint8_t *>(srs + n);           // n
+    for (int e = t; e < NB * n; e += blockDim.x) sab[e] = a.ab_g[(size_t)e * a.U];
+    for (int e = t; e < n; e += blockDim.x) {
+      srs[e] = a.rs_g[(size_t)e * a.U];
+      spv[e] = a.piv_g[(size_t)e * a.U];
+    }
+    __syncthreads();
+    ab = sab; piv = spv; rs = srs; stride = 1; scr = ssc;
+  }
   if (t < 2) {
     double2 *U = (t == 0) ? a.U_ring : a.W_ring;
     const double2 *L = (t == 0) ? a.lx_ring : a.lz_ring;
     const double *F = (t == 0) ? a.fx_ring : a.fz_ring;
-    double2 *sg = a.scratch + (size_t)t * NY;
-    double2 *yy = a.scratch + 2 * (size_t)NY + (size_t)t * a.n_g;
+    double2 *sg = scr + (size_t)t * NY;
+    double2 *yy = scr + 2 * (size_t)NY + (size_t)t * n;
     double2 *dd = a.dy1 + (size_t)t * NY;
     const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
     const double f0 = F[o0], f1 = F[o1], f2 = F[o2];
@@ -333,7 +352,7 @@ __global__ void k_mean(MeanArgs a) {
         acc.x += b * r.x;
         acc.y += b * r.y;
       }
-      const double sc = icg * a.rs_g[(size_t)p * a.U];
+      const double sc = icg * rs[(size_t)p * stride];
       return make_double2(acc.x * sc, acc.y * sc);
     };
     auto ys = [&](int p, double2 y) { yy[p] = y; };
@@ -356,7 +375,7 @@ __global__ void k_mean(MeanArgs a) {
         dd[jn] = make_double2(c11 * x.x, c11 * x.y);
       }
     };
-    band_solve<6, 6>(a.ab_g, a.piv_g, a.n_g, a.U, 0, rhs, ys, yl, out);
+    band_solve<6, 6>(ab, piv, n, stride, 0, rhs, ys, yl, out);
   }
   __syncthreads();
   const double2 *dU = a.dy1, *dW = a.dy1 + NY;
@@ -377,7 +396,22 @@ __global__ void k_mean(MeanArgs a) {
   }
 }
 
-void launch_mean(const MeanArgs &a, cudaStream_t st) { k_mean<<<1, 128, 0, st>>>(a); }
+size_t mean_smem_bytes(int NY, int n_g) {
+  return (2 * (size_t)NY + 2 * (size_t)n_g) * sizeof(double2) + 19 * (size_t)n_g * sizeof(double) +
+         (size_t)n_g * sizeof(double) + (size_t)n_g + 16;
+}
+
+// Opt in to the shared memory of the staged mean-mode solve when it fits.
+bool mean_prepare(int NY, int n_g) {
+  const size_t b = mean_smem_bytes(NY, n_g);
+  if (b > 200 * 1024) return false;
+  return cudaFuncSetAttribute(k_mean<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b) == cudaSuccess;
+}
+
+void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st) {
+  if (smem) k_mean<true><<<1, 256, mean_smem_bytes(a.NY, a.n_g), st>>>(a);
+  else k_mean<false><<<1, 128, 0, st>>>(a);
+}
 
 // ---------------------------------------------------------------------------
 // nonlinear_source (src/solver.cpp:240-260), one thread per mode:

@@ -83,6 +83,9 @@ struct XformArgs {
   int ring_mask;
   size_t fs;
   const long long *step;
+  // mixed precision: transform only the fluctuations (mode (0,0) left out)
+  // and add the mean-flow interaction terms in FP64 in the last kernel
+  int mean_split;
   double2 *out[3];
   void *zbuf;  // [6][NY][NZ2][NXH] complex<T>
   void *lbuf;  // [3][NY][NZ2][NXH] complex<T>
@@ -98,7 +101,8 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st);
 void launch_check_pattern(const double *ab, int n, int U, int *bad, cudaStream_t st);
 void launch_advance(long long *step, cudaStream_t st);
-void launch_mean(const MeanArgs &a, cudaStream_t st);
+void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st);
+bool mean_prepare(int NY, int n_g);
 void launch_nl(const NLArgs &a, cudaStream_t st);
 void launch_dapply(const DApplyArgs &a, cudaStream_t st);
 void launch_combine_y(double2 *out, const double2 *A, const double *ca, const double2 *B, const double *cb, int NY,

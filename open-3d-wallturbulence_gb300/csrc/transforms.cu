@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(1024) k_zback(XformArgs a) {
   __syncthreads();
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
     const int kz = idx / TX, c = idx - kz * TX;
-    if (i0 + c < d.NXH && kz != d.NZH) {
+    if (i0 + c < d.NXH && kz != d.NZH && !(a.mean_split && kz == 0 && i0 + c == 0)) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
       bufa[c * ls + slot] = from_d<T>(src[(size_t)kz * d.NXH + i0 + c]);
     }
@@ -141,6 +141,38 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   }
 }
 
+// Component f of Ubar x om(k) + u(k) x Obar at mode (kz, kx) and height j, in
+// FP64, where Ubar, Obar are the real parts of the (0, 0) modes (the mean flow
+// as the transforms see it) and the fields of the kx = 0 column enter through
+// their Hermitian part, as the real-part extraction of the x transform makes
+// them enter the physical product.  At (0, 0) it is Ubar x Obar.
+__device__ double2 mean_interaction(const XformArgs &a, int f, int j, int kz, int kx) {
+  const XformDims &d = a.d;
+  const int M = d.NZ * d.NXH;
+  const double2 *fld[6];
+  for (int q = 0; q < 6; ++q) {
+    const double2 *base = a.in[q];
+    if (a.ring_mask & (1 << q)) base += (size_t)ring_head(*a.step) * a.fs;
+    fld[q] = base + (size_t)j * M;
+  }
+  // mean vectors (u, v, w) and (ox, oy, oz): real parts of mode 0
+  double Ub[3], Ob[3];
+  for (int q = 0; q < 3; ++q) { Ub[q] = fld[q][0].x; Ob[q] = fld[3 + q][0].x; }
+  const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
+  if (kz == 0 && kx == 0) return make_double2(Ub[f1] * Ob[f2] - Ub[f2] * Ob[f1], 0.0);
+  auto val = [&](int q) -> double2 {
+    const double2 x = fld[q][(size_t)kz * d.NXH + kx];
+    if (kx != 0) return x;
+    const int kp = kz == 0 ? 0 : d.NZ - kz;
+    const double2 y = fld[q][(size_t)kp * d.NXH];
+    return make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
+  };
+  // (a x b)_f = a_f1 b_f2 - a_f2 b_f1
+  const double2 o1 = val(3 + f1), o2 = val(3 + f2), u1 = val(f1), u2 = val(f2);
+  return make_double2(Ub[f1] * o2.x - Ub[f2] * o1.x + u1.x * Ob[f2] - u2.x * Ob[f1],
+                      Ub[f1] * o2.y - Ub[f2] * o1.y + u1.y * Ob[f2] - u2.y * Ob[f1]);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
   constexpr int TX = XCfg<T>::TX;
@@ -164,7 +196,13 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
     if (i0 + c < d.NXH) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
       const double2 v = to_d(r[c * ls + slot]);
-      dst[(size_t)kz * d.NXH + i0 + c] = make_double2(v.x * sc, v.y * sc);
+      double2 o = make_double2(v.x * sc, v.y * sc);
+      if (a.mean_split && kz != d.NZH) {
+        const double2 l = mean_interaction(a, f, j, kz, i0 + c);
+        o.x += l.x;
+        o.y += l.y;
+      }
+      dst[(size_t)kz * d.NXH + i0 + c] = o;
     }
   }
 }
