@@ -101,7 +101,8 @@ int owt_create(const owt_params *params, owt_handle **out);
 int owt_destroy(owt_handle *h);
 
 /* Message of the last failed call on h; h == NULL gives the calling thread's
- * last owt_create failure. Never NULL. */
+ * last failure of a call that takes no handle (owt_create, owt_dy1_noalloc).
+ * Never NULL. */
 const char *owt_last_error(const owt_handle *h);
 
 /* init_fields (src/solver.cpp:329-426) with a caller-given velocity field in
@@ -185,6 +186,35 @@ int owt_get_info(const owt_handle *h, int what, int64_t *value);
 #define OWT_STAGE_LAMB 2
 #define OWT_STAGE_NONLINEAR 3
 int owt_enqueue_stage(owt_handle *h, int stage);
+
+/* DY1 along y for device arrays the caller owns, allocating no device memory.
+ * No counterpart in the reference: it is the compact first derivative of
+ * owt_dy_apply (order 1), out = diag(c11) A1^-1 B1 in, for callers that must
+ * not call cudaMalloc -- code running during CUDA graph capture, programs
+ * whose own pool allocator owns all device memory, and loops that cannot
+ * afford cudaMalloc's device-wide synchronisation.  It needs no handle.
+ *  - d_in, d_out: device pointers, 16-byte aligned, NY * nlines complex128
+ *    (interleaved), line index fastest: [y][line] (a whole field in the
+ *    library's device layout is nlines = NZ * NX/2).
+ *  - Grid: y = tanh(alpha_mesh s)/tanh(alpha_mesh), NY points.
+ *  - Scratch: a file-scope static device array of 256 KiB + 2 *
+ *    OWT_NOALLOC_MAX_VALUES * 16 bytes (32.25 MiB), held on every GPU that
+ *    loads the library until the process exits.  Requests beyond NY <=
+ *    OWT_NOALLOC_MAX_NY or NY * nlines <= OWT_NOALLOC_MAX_VALUES are rejected
+ *    with OWT_ERR_INVALID and a message in owt_last_error(NULL).
+ *  - The first call on a device looks up that array's device address (once
+ *    per device, with the device current); make that first call before any
+ *    stream capture.
+ *  - Every call rewrites everything it reads from the array (operators,
+ *    then scratch) before using it; calls share the array, so calls that can
+ *    overlap on the GPU (different streams without ordering) race.
+ *  - Asynchronous on `stream` (a cudaStream_t, NULL for the legacy default
+ *    stream); errors of the launch are returned, device-side ones appear at
+ *    the caller's next synchronisation. */
+#define OWT_NOALLOC_MAX_NY 1025
+#define OWT_NOALLOC_MAX_VALUES (1 << 20)
+int owt_dy1_noalloc(int64_t NY, int64_t nlines, double alpha_mesh, const double *d_in, double *d_out,
+                    void *stream);
 
 #ifdef __cplusplus
 }

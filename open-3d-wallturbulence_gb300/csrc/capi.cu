@@ -68,6 +68,8 @@ struct BandDev {
 
 }  // namespace
 
+void owt_set_thread_error(const std::string &m) { g_create_error = m; }
+
 struct owt_handle {
   std::string err;
   owt_params p{};

@@ -72,6 +72,7 @@ def load(path=LIB):
         "owt_enqueue_stage": ([_h, C.c_int], C.c_int),
         "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),
         "owt_get_info": ([_h, C.c_int, C.POINTER(C.c_int64)], C.c_int),
+        "owt_dy1_noalloc": ([C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
