@@ -91,25 +91,44 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # algorithmic work per stage (fixed formulas; see the design doc for derivations)
 # ---------------------------------------------------------------------------
-def stage_work(p):
+def stage_work(p, precision="fp64"):
+    """Algorithmic flops and bytes per launch of each kernel."""
     import math
     NY, M, NXH, NZ2, NX2 = p.NY, p.NZ * p.NXH, p.NXH, p.NZ2, p.NX2
-    S = 16.0 * NY * M  # bytes per spectral field
+    S = 16.0 * NY * M  # bytes per spectral field (complex128)
+    P = (16.0 if precision == "fp64" else 8.0) * NY * NZ2 * NXH  # one z-padded plane set
     # banded systems: v-system 5NY unknowns (kl 18, ku 15), omega_y-system 2NY (6, 6);
     # per column and complex rhs: 2 * 2 * (2 kl + ku) flops (forward + backward)
     fl_modes = M * (5 * NY * 4 * (2 * 18 + 15) + 2 * NY * 4 * (2 * 6 + 6) + 120 * NY)
     fl_fft = lambda n: 5.0 * n * math.log2(n)
-    n_z = 9 * NXH * NY                 # 6 backward + 3 forward z lines
-    n_x = 4.5 * NZ2 * NY               # 3 packed backward + 1.5 packed forward x lines
-    fl_lamb = n_z * fl_fft(NZ2) + n_x * fl_fft(NX2) + 9.0 * NX2 * NZ2 * NY
-    fl_nl = M * NY * 60.0
     unique = NXH * (p.NZ // 2 + 1)
     factor_bytes = 8.0 * unique * (5 * NY * (2 * 18 + 15 + 1) + 2 * NY * (2 * 6 + 6 + 1))
     return {
         "modes": {"flops": fl_modes, "bytes": 22 * S + factor_bytes},
-        "lamb": {"flops": fl_lamb, "bytes": 9 * S},
-        "nonlinear": {"flops": fl_nl, "bytes": 5 * S},
+        "zback": {"flops": 6 * NXH * NY * fl_fft(NZ2), "bytes": 6 * S + 6 * P},
+        "xlamb": {"flops": 4.5 * NZ2 * NY * fl_fft(NX2) + 9.0 * NX2 * NZ2 * NY, "bytes": 9 * P},
+        "zfwd": {"flops": 3 * NXH * NY * fl_fft(NZ2), "bytes": 3 * P + 3 * S},
+        "nonlinear": {"flops": M * NY * 60.0, "bytes": 5 * S},
     }
+
+
+# DRAM traffic per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+# of the 128x129x128 workload (profiles/k_xlamb_k_modes_channel180.md), scaled to
+# a launch at another size by the units the kernel processes (traffic grows in
+# proportion: y-z lines times kx modes for the transforms, modes times NY for the
+# mode kernel).
+NCU_TRAFFIC_128 = {"xlamb_fp64": 200.66e6, "modes": 1.647e9}
+
+
+def scaled_traffic(kernel, p, precision):
+    base = {"xlamb": "xlamb_fp64" if precision == "fp64" else None, "modes": "modes"}.get(kernel)
+    if not base or base not in NCU_TRAFFIC_128:
+        return None
+    if kernel == "xlamb":
+        units, units0 = p.NY * p.NZ2 * p.NXH, 129 * 192 * 64
+    else:
+        units, units0 = p.NY * p.NZ * p.NXH, 129 * 128 * 64
+    return NCU_TRAFFIC_128[base] * units / units0
 
 
 def measure_fp64_peak():
@@ -159,10 +178,7 @@ def run_ours(args, rank, world, local_rank):
     p = workload(args.workload)
     u, v, w = seeded_velocity(p, seed=0)
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
+    from owt.replicas import aggregate, barrier
 
     def timed_steps(solver, k):
         st = torch.cuda.ExternalStream(solver.stream)
@@ -173,16 +189,13 @@ def run_ours(args, rank, world, local_rank):
         e1.record(st)
         solver.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms, _ = aggregate(e0.elapsed_time(e1), k, device="cuda")
         return ms
 
     results = {}
     precisions = [args.precision] + [q for q in ("fp64", "mixed") if q != args.precision]
     solver = GpuSolver(p, precision=args.precision, device=local_rank)
+    tuning = solver.tuning_report()
     solver.init_fields(u, v, w)
     solver.use_graph(True)
     clocks = None
@@ -225,7 +238,7 @@ def run_ours(args, rank, world, local_rank):
         solver.init_fields(u, v, w)
         st = torch.cuda.ExternalStream(solver.stream)
         reps = max(3, min(10, args.steps))
-        for name, sid in (("modes", 0), ("lamb", 2), ("nonlinear", 3)):
+        for name, sid in (("modes", 0), ("zback", 4), ("xlamb", 5), ("zfwd", 6), ("nonlinear", 3)):
             solver.enqueue_stage(sid)
             solver.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -276,12 +289,8 @@ def run_ours(args, rank, world, local_rank):
             solver.get("vory", out=out_g)
             solver.friction()
         barrier()
-        dt_e2e = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([dt_e2e], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt_e2e = float(t.item())
-        e2e = {"value": world * k_e2e / dt_e2e, "unit": "steps/s", "h2d_bytes_per_step": int(bi),
+        dt_ms, e2e_rate = aggregate((time.perf_counter() - t0) * 1e3, k_e2e, device="cuda")
+        e2e = {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": int(bi),
                "d2h_bytes_per_step": int(bo)}
     solver.close()
 
@@ -292,18 +301,21 @@ def run_ours(args, rank, world, local_rank):
 
     peaks, peak_kind = load_peaks()
     fp64_peak = measure_fp64_peak()
-    work = stage_work(p)
-    dom = max(("modes", "lamb", "nonlinear"), key=lambda n: stage_ms.get(n, 0.0))
+    work = stage_work(p, args.precision)
+    dom = max(stage_ms, key=lambda n: stage_ms[n])
     t_dom = stage_ms[dom] * 1e-3
     fl_dom = work[dom]["flops"]
-    if args.precision == "mixed" and dom == "lamb":
+    if args.precision == "mixed" and dom in ("zback", "xlamb", "zfwd"):
         roof = {"bound": "hbm", "achieved": work[dom]["bytes"] / t_dom / 1e9, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s"}
     else:
         roof = {"bound": "fp64", "achieved": fl_dom / t_dom / 1e12, "peak": fp64_peak, "unit": "TFLOP/s"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["kernel"] = dom
-    roof["traffic"] = None
+    roof["kernel"] = {"modes": "k_modes", "zback": "k_zback", "xlamb": "k_xlamb", "zfwd": "k_zfwd",
+                      "nonlinear": "k_nl"}[dom]
+    roof["traffic"] = scaled_traffic(dom, p, args.precision)
+    roof["algorithmic_bytes"] = work[dom]["bytes"]
+    roof["traffic_source"] = "ncu at 128x129x128, scaled by units processed (profiles/)"
     roof["peak_source"] = ("cuBLAS DGEMM (torch.matmul float64, 4096^3) measured in this run"
                            if roof["bound"] == "fp64" else f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})")
     roof["stage_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
@@ -332,6 +344,7 @@ def run_ours(args, rank, world, local_rank):
             "parallelism": "replicas" if world > 1 else "single",
             "l2": "inputs larger than L2 (the step streams ~40 GB of state and factors)",
             "grid_point_updates_per_s": round(value * p.NX2 * p.NZ2 * p.NY, 1),
+            "mode_kernel_autotune": tuning,
         },
         "variants": {q: {"steps_per_s": round(world * r["steps_per_s"], 4), "ms_per_step": round(r["ms_per_step"], 4)}
                      for q, r in results.items()},
@@ -354,6 +367,83 @@ def run_ours(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------
 # CPU arm: the reference algorithm (oracle restatement) on the host cores
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# batch workload: 64 uneven minimal channels, one graph launch per step
+# ---------------------------------------------------------------------------
+def run_batch(args, rank, world, local_rank):
+    import torch
+    from owt.batch import Batch, minimal_channels
+    from owt.ic import seeded_velocity
+    from owt.replicas import aggregate, barrier
+    from owt.solver import GpuSolver
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ps = minimal_channels(64, seed=0)
+    solvers = []
+    for q, p in enumerate(ps):
+        s = GpuSolver(p, precision="mixed", device=local_rank)
+        s.init_fields(*seeded_velocity(p, seed=q))
+        s.use_graph(True)
+        solvers.append(s)
+    points = sum(p.NX2 * p.NZ2 * p.NY for p in ps)
+    # serial loop: one channel after another, each its own graph
+    for s in solvers:
+        s.time_Integration(args.warmup)
+        s.synchronize()
+    k_loop = max(2, args.steps // 4)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(k_loop):
+        for s in solvers:
+            s.time_Integration(1)
+            s.synchronize()
+    barrier()
+    loop_ms, loop_rate = aggregate((time.perf_counter() - t0) * 1e3, 64 * k_loop, device="cuda")
+    # batched: all channels as branches of one graph
+    b = Batch(solvers)
+    b.step(args.warmup)
+    b.synchronize()
+    st = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = sum(s.launch_count for s in solvers)
+    with ClockSampler(local_rank) as cs:
+        barrier()
+        e0.record(st)
+        b.step(args.steps)
+        e1.record(st)
+        b.synchronize()
+        barrier()
+    ms, rate = aggregate(e0.elapsed_time(e1), 64 * args.steps, device="cuda")
+    launches = sum(s.launch_count for s in solvers) - l0
+    variants = {}
+    for s in solvers:
+        v = s.tuning_report().split("-> ")[-1]
+        variants[v] = variants.get(v, 0) + 1
+    b.close()
+    for s in solvers:
+        s.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": "channel-steps/s, 64 uneven minimal channels (Re_tau 150-250), one graph launch per step",
+        "value": round(rate, 3), "unit": "channel-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic: 64 seeded minimal channels, laminar + seeded perturbation each",
+        "config": {"workload": "batch64_minimal_channels", "precision": "mixed", "channels": 64,
+                   "physical_points_total": points, "mode_kernel_variants": variants,
+                   "l2": "no flush; per-step state of all channels ~%.1f GB" % (
+                       sum(22 * 16 * p.NY * p.NZ * p.NXH for p in ps) / 1e9)},
+        "variants": {"serial_loop": {"channel_steps_per_s": round(loop_rate, 3),
+                                     "ms_per_step_all_channels": round(loop_ms / k_loop, 4)},
+                     "speedup_vs_serial_loop": round(rate / loop_rate, 3)},
+        "gpu_launches": launches,
+        "clocks": cs.summary(),
+    }
+
+
 def build_port():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
 
@@ -421,7 +511,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--workload", choices=["channel_550", "channel_180"], default="channel_550")
+    ap.add_argument("--workload", choices=["channel_550", "channel_180", "batch64"], default="channel_550")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -429,6 +519,8 @@ def main():
     rank, world, local_rank = dist_env()
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload == "batch64":
+        line = run_batch(args, rank, world, local_rank)
     else:
         line = run_ours(args, rank, world, local_rank)
     if line is not None and rank == 0:

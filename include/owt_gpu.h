@@ -158,6 +158,38 @@ int owt_get_launch_count(const owt_handle *h, int64_t *count);
 int owt_get_grid(const owt_handle *h, double *y);
 int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
 
+/* Batches of independent channels (no counterpart in the reference, which runs
+ * one channel per MPI job).  A batch captures one time step of every handle
+ * as parallel branches of a single CUDA graph, so a step of all channels is
+ * one graph launch and small channels run concurrently on the GPU.  Handles
+ * keep their own state, sizes and parameters (uneven sizes are fine) and
+ * must outlive the batch; all must be on one device and initialised.  While
+ * a handle is in a batch, step it through the batch only. */
+typedef struct owt_batch owt_batch;
+int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out);
+int owt_batch_step(owt_batch *b, int64_t nsteps);
+int owt_batch_synchronize(owt_batch *b);
+int owt_batch_get_stream(const owt_batch *b, void **stream);
+int owt_batch_destroy(owt_batch *b);
+
+/* Wall-normal statistics of the current velocity (no counterpart in the
+ * reference, which computes none).  out[q * NY + j] for q = 0..6:
+ * mean U, V, W (real parts of the (0,0) modes), RMS of u', v', w', and the
+ * Reynolds shear stress <u'v'>, all as averages over x and z of the physical
+ * fields the transforms produce (Parseval: kx > 0 modes count twice, the
+ * kx = 0 column through its Hermitian part, the Nyquist kz row not at all). */
+int owt_statistics(owt_handle *h, double *out7ny);
+
+/* Full-state checkpoint for an exact restart (the reference has none,
+ * README.md:11; its snapshots hold u, v, w only).  The image holds the
+ * parameters, the step counter, every history level (v, omega_y, Hv, Hg and
+ * the DY2 v history), the current u, w, omega_x, omega_z and Lamb vector, the
+ * mean-mode and friction histories, in the device layout.  Restoring it and
+ * stepping reproduces the uninterrupted run bit for bit. */
+int owt_checkpoint_bytes(const owt_handle *h, int64_t *bytes);
+int owt_checkpoint_save(owt_handle *h, void *host, int64_t bytes);
+int owt_checkpoint_load(owt_handle *h, const void *host, int64_t bytes);
+
 /* Options and introspection (no counterpart in the reference).
  * OWT_OPT_FORCE_DENSE_BANDS: 1 = sweep the full band of the v-system in every
  *   column instead of skipping structurally-zero interior entries (the two
@@ -165,13 +197,22 @@ int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
  * OWT_INFO_SPARSE_SOLVE: 1 if the interior-sparse v-system solve is active.
  * OWT_INFO_PATTERN_VIOLATIONS: modes whose factors fell outside the sparse
  *   pattern at setup (any such mode selects the full-band solve).
- * OWT_INFO_DEVICE_BYTES: device memory held by the handle. */
+ * OWT_INFO_DEVICE_BYTES: device memory held by the handle.
+ * Autotuning: owt_create times every variant of the mode kernel (thread
+ * mapping, block shape, register budget; bitwise-identical results) and keeps
+ * the fastest.  OWT_INFO_MODES_VARIANT is the variant in use,
+ * OWT_INFO_MODES_VARIANTS their number, OWT_OPT_MODES_VARIANT forces one
+ * (-1 returns to the tuned choice), owt_tuning_report() lists the timings. */
 #define OWT_OPT_FORCE_DENSE_BANDS 1
+#define OWT_OPT_MODES_VARIANT 2
 #define OWT_INFO_SPARSE_SOLVE 1
 #define OWT_INFO_PATTERN_VIOLATIONS 2
 #define OWT_INFO_DEVICE_BYTES 3
+#define OWT_INFO_MODES_VARIANT 4
+#define OWT_INFO_MODES_VARIANTS 5
 int owt_set_option(owt_handle *h, int option, int64_t value);
 int owt_get_info(const owt_handle *h, int what, int64_t *value);
+const char *owt_tuning_report(const owt_handle *h);
 
 /* Measurement aid, no counterpart in the reference: enqueue one stage of the
  * step on the handle's stream without advancing the step counter, so a caller
@@ -180,11 +221,16 @@ int owt_get_info(const owt_handle *h, int what, int64_t *value);
  *   0: mode kernel (RHS assembly, both implicit solves, solve_horizontal)
  *   1: mean mode (solve_mean + friction)
  *   2: transforms + products (Lamb vector, three kernels)
- *   3: nonlinear source */
+ *   3: nonlinear source
+ *   4, 5, 6: the three transform kernels alone (z backward, x pass with the
+ *            products, z forward) */
 #define OWT_STAGE_MODES 0
 #define OWT_STAGE_MEAN 1
 #define OWT_STAGE_LAMB 2
 #define OWT_STAGE_NONLINEAR 3
+#define OWT_STAGE_ZBACK 4
+#define OWT_STAGE_XLAMB 5
+#define OWT_STAGE_ZFWD 6
 int owt_enqueue_stage(owt_handle *h, int stage);
 
 /* DY1 along y for device arrays the caller owns, allocating no device memory.

@@ -301,9 +301,12 @@ struct owt_handle {
         (axis == 0 ? twx : twz)[prec] = d;
       }
     }
-    ck(cudaMemsetAsync(v_ring, 0, 3 * fs * sizeof(double2), st), "memset");
-    ck(cudaMemsetAsync(g_ring, 0, 3 * fs * sizeof(double2), st), "memset");
+    for (double2 *ring : {v_ring, g_ring, hv_ring, hg_ring, q_ring})
+      ck(cudaMemsetAsync(ring, 0, 3 * fs * sizeof(double2), st), "memset");
+    for (double2 *f : {u, w, ox, oz, lx, ly, lz})
+      ck(cudaMemsetAsync(f, 0, fs * sizeof(double2), st), "memset");
     ck(cudaStreamSynchronize(st), "setup");
+    autotune_modes();
   }
 
   // ---- kernel sequences --------------------------------------------------------
@@ -371,7 +374,8 @@ struct owt_handle {
     a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
     a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg;
     a.step = d_step;
-    launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense, st);
+    launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense,
+                 forced_variant >= 0 ? forced_variant : modes_variant, st);
   }
   void stage_mean() {
     MeanArgs ma{};
@@ -416,6 +420,43 @@ struct owt_handle {
   int64_t per_step_launches = 0;
   bool force_dense = false;  // testing aid: always sweep the full band
   bool mean_smem = false;    // staged mean-mode solve in shared memory
+  int modes_variant = 0;     // chosen by the autotuner
+  int forced_variant = -1;   // testing aid: run this variant instead
+  std::string tuning;        // autotuner report
+
+  // Autotuner: time every mode-kernel variant on the (zero) state, keep the
+  // fastest.  Variants differ only in thread mapping and block shape; their
+  // results are bitwise identical, so the choice affects speed only.
+  void autotune_modes() {
+    modes_variant = 0;
+    tuning.clear();
+    if (!sparse_v) { tuning = "full-band solve (no variants)"; return; }
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    for (int v = 0; v < modes_variant_count(); ++v) {
+      forced_variant = v;
+      stage_modes();  // warm-up
+      ck(cudaEventRecord(e0, st), "event");
+      for (int r = 0; r < 2; ++r) stage_modes();
+      ck(cudaEventRecord(e1, st), "event");
+      ck(cudaEventSynchronize(e1), "event");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+      ms *= 0.5f;
+      launches += 3;
+      char buf[96];
+      std::snprintf(buf, sizeof(buf), "%s%s=%.3fms", tuning.empty() ? "" : " ", modes_variant_name(v), ms);
+      tuning += buf;
+      if (ms < best) { best = ms; modes_variant = v; }
+    }
+    forced_variant = -1;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_launch("autotune");
+    tuning += std::string(" -> ") + modes_variant_name(modes_variant);
+  }
 
   void drop_graph() {
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
@@ -752,14 +793,223 @@ int owt_get_grid(const owt_handle *h, double *y) {
   return OWT_OK;
 }
 
-int owt_set_option(owt_handle *h, int option, int64_t value) {
+struct owt_batch {
+  std::vector<owt_handle *> hs;
+  cudaStream_t st = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaEvent_t> events;
+  ~owt_batch() {
+    if (st) cudaStreamSynchronize(st);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
+  if (!handles || count < 1 || !out) {
+    g_create_error = "owt_batch_create: need at least one handle";
+    return OWT_ERR_INVALID;
+  }
+  *out = nullptr;
+  owt_batch *b = new owt_batch();
+  try {
+    for (int q = 0; q < count; ++q) {
+      owt_handle *h = handles[q];
+      if (!h || !h->initialized) throw OwtError(OWT_ERR_STATE, "every handle must be initialised");
+      if (h->p.device != handles[0]->p.device) throw OwtError(OWT_ERR_INVALID, "handles on different devices");
+      ck(cudaStreamSynchronize(h->st), "batch");
+      h->recompute_dirty_q();
+      b->hs.push_back(h);
+    }
+    ck(cudaSetDevice(handles[0]->p.device), "cudaSetDevice");
+    ck(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking), "stream");
+    b->events.resize(2 * count + 1);
+    for (auto &e : b->events) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    // fork: every handle's stream waits on the batch stream, enqueues its
+    // step, and the batch stream joins them all
+    ck(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    ck(cudaEventRecord(b->events[0], b->st), "fork");
+    for (int q = 0; q < count; ++q) {
+      owt_handle *h = b->hs[q];
+      ck(cudaStreamWaitEvent(h->st, b->events[0], 0), "fork wait");
+      h->enqueue_step();
+      ck(cudaEventRecord(b->events[1 + q], h->st), "join");
+      ck(cudaStreamWaitEvent(b->st, b->events[1 + q], 0), "join wait");
+    }
+    ck(cudaStreamEndCapture(b->st, &b->graph), "end capture");
+    ck(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate");
+    for (owt_handle *h : b->hs) h->check_launch("batch capture");
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    cudaGetLastError();
+    delete b;
+    return OWT_ERR_CUDA;
+  }
+  *out = b;
+  return OWT_OK;
+}
+
+int owt_batch_step(owt_batch *b, int64_t nsteps) {
+  if (!b || nsteps < 0) return OWT_ERR_INVALID;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    if (cudaGraphLaunch(b->exec, b->st) != cudaSuccess) {
+      g_create_error = "batch graph launch failed";
+      return OWT_ERR_CUDA;
+    }
+    for (owt_handle *h : b->hs) {
+      ++h->steps;
+      h->launches += 7;
+    }
+  }
+  return OWT_OK;
+}
+
+int owt_batch_synchronize(owt_batch *b) {
+  if (!b) return OWT_ERR_INVALID;
+  if (cudaStreamSynchronize(b->st) != cudaSuccess) {
+    g_create_error = "batch synchronize failed";
+    return OWT_ERR_CUDA;
+  }
+  for (owt_handle *h : b->hs) {
+    const int rc = owt_synchronize(h);
+    if (rc != OWT_OK) {
+      g_create_error = owt_last_error(h);
+      return rc;
+    }
+  }
+  return OWT_OK;
+}
+
+int owt_batch_get_stream(const owt_batch *b, void **stream) {
+  if (!b || !stream) return OWT_ERR_INVALID;
+  *stream = (void *)b->st;
+  return OWT_OK;
+}
+
+int owt_batch_destroy(owt_batch *b) {
+  delete b;
+  return OWT_OK;
+}
+
+int owt_statistics(owt_handle *h, double *out7ny) {
   return guard(h, [&] {
-    if (option != OWT_OPT_FORCE_DENSE_BANDS) throw OwtError(OWT_ERR_INVALID, "unknown option");
-    ck(cudaStreamSynchronize(h->st), "set option");
-    h->drop_graph();
-    h->force_dense = value != 0;
+    if (!out7ny) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    double *d = reinterpret_cast<double *>(h->tmpA);  // 7 NY doubles fit easily
+    launch_stats(h->u, h->ring_level(h->v_ring, 0), h->w, h->NY, h->NZ, h->NXH, d, h->st);
+    ++h->launches;
+    h->check_launch("statistics");
+    ck(cudaMemcpyAsync(out7ny, d, 7 * (size_t)h->NY * sizeof(double), cudaMemcpyDeviceToHost, h->st), "D2H");
+    h->sync_and_check();
   });
 }
+
+// Checkpoint image: header, then fields in level order (independent of the
+// ring slots), then the NY-vectors and scalars.
+namespace {
+struct CkptHeader {
+  char magic[8];
+  int64_t version, NX, NY, NZ, step, precision;
+  double dt, dkx, dkz, alpha_mesh, nu;
+};
+const int kRings = 5, kFields = 7;
+}  // namespace
+
+int owt_checkpoint_bytes(const owt_handle *h, int64_t *bytes) {
+  if (!h || !bytes) return OWT_ERR_INVALID;
+  const size_t f = h->fs * sizeof(double2), v = (size_t)h->NY * sizeof(double2);
+  *bytes = (int64_t)(sizeof(CkptHeader) + (3 * kRings + kFields) * f + 12 * v + 6 * sizeof(double));
+  return OWT_OK;
+}
+
+int owt_checkpoint_save(owt_handle *h, void *host, int64_t bytes) {
+  return guard(h, [&] {
+    int64_t need = 0;
+    owt_checkpoint_bytes(h, &need);
+    if (!host || bytes < need) throw OwtError(OWT_ERR_INVALID, "checkpoint buffer too small");
+    ck(cudaStreamSynchronize(h->st), "checkpoint");
+    h->recompute_dirty_q();
+    CkptHeader hd{};
+    std::memcpy(hd.magic, "OWTCKPT1", 8);
+    hd.version = 1; hd.NX = h->NX; hd.NY = h->NY; hd.NZ = h->NZ; hd.step = h->steps; hd.precision = h->precision;
+    hd.dt = h->p.dt; hd.dkx = h->p.dkx; hd.dkz = h->p.dkz; hd.alpha_mesh = h->p.alpha_mesh; hd.nu = h->p.nu;
+    char *o = static_cast<char *>(host);
+    std::memcpy(o, &hd, sizeof(hd));
+    o += sizeof(hd);
+    const size_t f = h->fs * sizeof(double2), v = (size_t)h->NY * sizeof(double2);
+    for (double2 *ring : {h->v_ring, h->g_ring, h->hv_ring, h->hg_ring, h->q_ring})
+      for (int l = 0; l < 3; ++l, o += f)
+        ck(cudaMemcpyAsync(o, h->ring_level(ring, l), f, cudaMemcpyDeviceToHost, h->st), "D2H");
+    for (double2 *fld : {h->u, h->w, h->ox, h->oz, h->lx, h->ly, h->lz}) {
+      ck(cudaMemcpyAsync(o, fld, f, cudaMemcpyDeviceToHost, h->st), "D2H");
+      o += f;
+    }
+    for (double2 *ring : {h->lxm_ring, h->lzm_ring, h->U_ring, h->W_ring})
+      for (int l = 0; l < 3; ++l, o += v)
+        ck(cudaMemcpyAsync(o, ring + (size_t)h->slot(l) * h->NY, v, cudaMemcpyDeviceToHost, h->st), "D2H");
+    for (double *fr : {h->fx_ring, h->fz_ring})
+      for (int l = 0; l < 3; ++l, o += sizeof(double))
+        ck(cudaMemcpyAsync(o, fr + h->slot(l), sizeof(double), cudaMemcpyDeviceToHost, h->st), "D2H");
+    ck(cudaStreamSynchronize(h->st), "checkpoint");
+  });
+}
+
+int owt_checkpoint_load(owt_handle *h, const void *host, int64_t bytes) {
+  return guard(h, [&] {
+    int64_t need = 0;
+    owt_checkpoint_bytes(h, &need);
+    if (!host || bytes < need) throw OwtError(OWT_ERR_INVALID, "checkpoint image too small");
+    CkptHeader hd;
+    std::memcpy(&hd, host, sizeof(hd));
+    if (std::memcmp(hd.magic, "OWTCKPT1", 8) != 0 || hd.version != 1)
+      throw OwtError(OWT_ERR_INVALID, "not a checkpoint image of this library");
+    if (hd.NX != h->NX || hd.NY != h->NY || hd.NZ != h->NZ || hd.dt != h->p.dt || hd.dkx != h->p.dkx ||
+        hd.dkz != h->p.dkz || hd.alpha_mesh != h->p.alpha_mesh || hd.nu != h->p.nu)
+      throw OwtError(OWT_ERR_INVALID, "checkpoint parameters differ from the handle's");
+    ck(cudaStreamSynchronize(h->st), "restore");
+    h->drop_graph();
+    h->steps = hd.step;
+    const long long dstep = (long long)hd.step;
+    ck(cudaMemcpyAsync(h->d_step, &dstep, sizeof(dstep), cudaMemcpyHostToDevice, h->st), "H2D");
+    const char *o = static_cast<const char *>(host) + sizeof(hd);
+    const size_t f = h->fs * sizeof(double2), v = (size_t)h->NY * sizeof(double2);
+    for (double2 *ring : {h->v_ring, h->g_ring, h->hv_ring, h->hg_ring, h->q_ring})
+      for (int l = 0; l < 3; ++l, o += f)
+        ck(cudaMemcpyAsync(h->ring_level(ring, l), o, f, cudaMemcpyHostToDevice, h->st), "H2D");
+    for (double2 *fld : {h->u, h->w, h->ox, h->oz, h->lx, h->ly, h->lz}) {
+      ck(cudaMemcpyAsync(fld, o, f, cudaMemcpyHostToDevice, h->st), "H2D");
+      o += f;
+    }
+    for (double2 *ring : {h->lxm_ring, h->lzm_ring, h->U_ring, h->W_ring})
+      for (int l = 0; l < 3; ++l, o += v)
+        ck(cudaMemcpyAsync(ring + (size_t)h->slot(l) * h->NY, o, v, cudaMemcpyHostToDevice, h->st), "H2D");
+    for (double *fr : {h->fx_ring, h->fz_ring})
+      for (int l = 0; l < 3; ++l, o += sizeof(double))
+        ck(cudaMemcpyAsync(fr + h->slot(l), o, sizeof(double), cudaMemcpyHostToDevice, h->st), "H2D");
+    h->q_dirty[0] = h->q_dirty[1] = h->q_dirty[2] = false;
+    h->initialized = true;
+    ck(cudaStreamSynchronize(h->st), "restore");
+  });
+}
+
+int owt_set_option(owt_handle *h, int option, int64_t value) {
+  return guard(h, [&] {
+    ck(cudaStreamSynchronize(h->st), "set option");
+    h->drop_graph();
+    if (option == OWT_OPT_FORCE_DENSE_BANDS) {
+      h->force_dense = value != 0;
+    } else if (option == OWT_OPT_MODES_VARIANT) {
+      if (value < -1 || value >= modes_variant_count()) throw OwtError(OWT_ERR_INVALID, "no such variant");
+      h->forced_variant = (int)value;
+    } else {
+      throw OwtError(OWT_ERR_INVALID, "unknown option");
+    }
+  });
+}
+
+const char *owt_tuning_report(const owt_handle *h) { return h ? h->tuning.c_str() : ""; }
 
 int owt_get_info(const owt_handle *h, int what, int64_t *value) {
   if (!h || !value) return OWT_ERR_INVALID;
@@ -767,6 +1017,8 @@ int owt_get_info(const owt_handle *h, int what, int64_t *value) {
     case OWT_INFO_SPARSE_SOLVE: *value = (h->sparse_v && !h->force_dense) ? 1 : 0; return OWT_OK;
     case OWT_INFO_PATTERN_VIOLATIONS: *value = h->pattern_violations; return OWT_OK;
     case OWT_INFO_DEVICE_BYTES: *value = (int64_t)h->device_bytes; return OWT_OK;
+    case OWT_INFO_MODES_VARIANT: *value = h->forced_variant >= 0 ? h->forced_variant : h->modes_variant; return OWT_OK;
+    case OWT_INFO_MODES_VARIANTS: *value = modes_variant_count(); return OWT_OK;
     default: return OWT_ERR_INVALID;
   }
 }
@@ -779,6 +1031,10 @@ int owt_enqueue_stage(owt_handle *h, int stage) {
       case OWT_STAGE_MEAN: h->stage_mean(); h->launches += 1; break;
       case OWT_STAGE_LAMB: h->launches += launch_lamb(h->xform_args(), h->precision, h->st); break;
       case OWT_STAGE_NONLINEAR: launch_nl(h->nl_args(true), h->st); h->launches += 1; break;
+      case OWT_STAGE_ZBACK: case OWT_STAGE_XLAMB: case OWT_STAGE_ZFWD:
+        launch_lamb_part(h->xform_args(), h->precision, stage - OWT_STAGE_ZBACK, h->st);
+        h->launches += 1;
+        break;
       default: throw OwtError(OWT_ERR_INVALID, "unknown stage");
     }
     h->check_launch("stage");

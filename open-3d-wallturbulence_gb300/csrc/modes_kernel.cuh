@@ -1,0 +1,181 @@
+// The mode kernel (RHS assembly, both implicit solves, solve_horizontal's
+// components) as a template; instantiated by modes_pair.cu / modes_quad.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "owt_device.cuh"
+#include "solve_kernels.h"
+
+namespace owt {
+
+// ---------------------------------------------------------------------------
+// Mode kernel: two threads per Fourier mode (one per real component).  For
+// mode (kz, kx):
+//  1. source_g = sum beta Hg_l + sum alpha g_l / dt      (solver.cpp:573-574)
+//  2. omega_y-system: g and DY1 g                         (solver.cpp:578, 603)
+//  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
+//     with DY2 v_l kept as a history of its own (q_l)    (solver.cpp:569-571)
+//  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
+//  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
+// ---------------------------------------------------------------------------
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
+  // One thread per real component of a mode (the band systems are real).
+  // Pair mapping: lanes 2m, 2m+1 are Re, Im of mode m.  Quad mapping: lanes
+  // 4u..4u+3 are (Re, Im) of the two modes +kz, -kz of unique mode u, which
+  // share one factorization, so four adjacent lanes read the same factors.
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  int m, comp, k, i, kabs;
+  if (QUAD) {
+    const int uq = tid >> 2, r = tid & 3, sgn = r >> 1;
+    comp = r & 1;
+    if (uq >= a.U) return;
+    kabs = uq / a.NXH;
+    i = uq - kabs * a.NXH;
+    if (sgn == 1 && (kabs == 0 || kabs == a.NZH)) return;  // these have no -kz partner
+    k = sgn == 0 ? kabs : a.NZ - kabs;
+    m = k * a.NXH + i;
+  } else {
+    m = tid >> 1;
+    comp = tid & 1;
+    if (m >= a.M) return;
+    k = m / a.NXH;
+    i = m - k * a.NXH;
+    kabs = (k <= a.NZH) ? k : a.NZ - k;
+  }
+  const int M = a.M, NY = a.NY;
+  const int u = kabs * a.NXH + i;
+  const double kx = a.kx[i], kz = a.kz[k];
+  const double k2 = kx * kx + kz * kz;
+  const long long s = *a.step;
+  const int h = ring_head(s);
+  const size_t fs2 = 2 * (size_t)NY * M;  // doubles per field
+  auto lvl = [&](const double2 *ring, int l) {
+    return reinterpret_cast<const double *>(ring) + (size_t)((h + l) % 3) * fs2 + comp;
+  };
+  const double *v0 = lvl(a.v_ring, 0), *v1 = lvl(a.v_ring, 1), *v2 = lvl(a.v_ring, 2);
+  const double *g0 = lvl(a.g_ring, 0), *g1 = lvl(a.g_ring, 1), *g2 = lvl(a.g_ring, 2);
+  const double *hv0 = lvl(a.hv_ring, 0), *hv1 = lvl(a.hv_ring, 1), *hv2 = lvl(a.hv_ring, 2);
+  const double *hg0 = lvl(a.hg_ring, 0), *hg1 = lvl(a.hg_ring, 1), *hg2 = lvl(a.hg_ring, 2);
+  const double *q0 = lvl(a.q_ring, 0), *q1 = lvl(a.q_ring, 1), *q2 = lvl(a.q_ring, 2);
+  const int hn = (h + 2) % 3;  // slot of the new level 0
+  double *vn = reinterpret_cast<double *>(a.v_ring) + (size_t)hn * fs2 + comp;
+  double *gn = reinterpret_cast<double *>(a.g_ring) + (size_t)hn * fs2 + comp;
+  double *qn = reinterpret_cast<double *>(a.q_ring) + (size_t)hn * fs2 + comp;
+  double *sg = reinterpret_cast<double *>(a.sg) + comp;
+  double *dg = reinterpret_cast<double *>(a.dg) + comp;
+  double *yv = reinterpret_cast<double *>(a.yv) + comp;
+  double *yg = reinterpret_cast<double *>(a.yg) + comp;
+  auto E = [&](int j) { return 2 * ((size_t)j * M + m); };  // offset of (j, m) in doubles
+  const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
+  const double idt = a.inv_dt;
+
+  // 1. source_g, walls zero (solver.cpp:573-574, 598-599)
+  for (int j = 0; j < NY; ++j) {
+    const size_t e = E(j);
+    double r = 0.0;
+    if (j != 0 && j != NY - 1)
+      r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
+    sg[e] = r;
+  }
+
+  // 2. omega_y-system: g and DY1 g
+  const double icg = a.inv_cg[u];
+  {
+    double d2 = 0.0;
+    auto rhs = [&](int p) -> double {
+      double acc = 0.0;
+#pragma unroll
+      for (int q = 0; q < 5; ++q) acc += a.rb_val[p * 5 + q] * sg[E(a.rb_col[p * 5 + q])];
+      return acc * (icg * a.rs_g[(size_t)p * a.U + u]);
+    };
+    auto ys = [&](int p, double y) { yg[E(p)] = y; };
+    auto yl = [&](int p) -> double { return yg[E(p)]; };
+    auto out = [&](int c, double x) {
+      const int jn = c >> 1;
+      if (c & 1) {
+        d2 = x * a.inv_h2;
+      } else {
+        x *= a.inv_h;
+        const size_t e = E(jn);
+        double g = 0.0;
+        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nu * a.c21[jn] * x + a.nu * a.c22[jn] * d2) * icg;
+        gn[e] = g;
+        dg[e] = a.c11[jn] * x;
+      }
+    };
+    band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
+  }
+  __syncwarp(__activemask());  // the partner's g, DY1 g are read below
+
+  // 3-5. v-system, then solve_horizontal's components
+  {
+    const double k2dt = k2 * idt;
+    const bool horiz = !(k2 < 1.e-8);
+    const double ik2 = horiz ? 1.0 / k2 : 0.0;
+    const double ax = kx * ik2, az = kz * ik2;
+    const double kzk2 = kz * k2, kxk2 = kx * k2;
+    double d1 = 0.0, d2 = 0.0;
+    auto rhs = [&](int p) -> double {
+      const int j = a.rhs_node_v[p];
+      if (j < 0) return 0.0;
+      const size_t e = E(j);
+      const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
+      const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
+      const double r = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
+      return r * a.rs_v[(size_t)p * a.U + u];
+    };
+    auto ys = [&](int p, double y) { yv[E(p)] = y; };
+    auto yl = [&](int p) -> double { return yv[E(p)]; };
+    auto out = [&](int c, double x) {
+      const int jn = c / 5, t = c - 5 * jn;
+      if (t == 2) {
+        d2 = x * a.inv_h2;
+      } else if (t == 1) {
+        d1 = x * a.inv_h;
+      } else if (t == 0) {
+        const size_t e = E(jn);
+        vn[e] = x;
+        const double q = a.c21[jn] * d1 + a.c22[jn] * d2;
+        qn[e] = q;
+        if (horiz) {
+          const double dv = a.c11[jn] * d1;
+          const unsigned mask = __activemask();
+          const double xo = __shfl_xor_sync(mask, x, 1), dvo = __shfl_xor_sync(mask, dv, 1),
+                       qo = __shfl_xor_sync(mask, q, 1);
+          // full complex values (re, im) of v, DY1 v, DY2 v, g, DY1 g
+          const double vr = comp ? xo : x, vi = comp ? x : xo;
+          const double dvr = comp ? dvo : dv, dvi = comp ? dv : dvo;
+          const double qr = comp ? qo : q, qi = comp ? q : qo;
+          const double *gp = gn - comp, *dgp = dg - comp;
+          const double gr = gp[e], gi = gp[e + 1], dgr = dgp[e], dgi = dgp[e + 1];
+          // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
+          // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
+          const double ur = -ax * dvi + az * gi, ui = ax * dvr - az * gr;
+          const double wr = -ax * gi - az * dvi, wi = ax * gr + az * dvr;
+          const double tx = kx * dgr + kz * qr - kzk2 * vr, ty = kx * dgi + kz * qi - kzk2 * vi;
+          const double sx = kz * dgr - kx * qr + kxk2 * vr, sy = kz * dgi - kx * qi + kxk2 * vi;
+          double *uo = reinterpret_cast<double *>(a.u_out), *wo = reinterpret_cast<double *>(a.w_out);
+          double *oxo = reinterpret_cast<double *>(a.ox_out), *ozo = reinterpret_cast<double *>(a.oz_out);
+          uo[e + comp] = comp ? ui : ur;
+          wo[e + comp] = comp ? wi : wr;
+          oxo[e + comp] = comp ? tx * ik2 : -ty * ik2;
+          ozo[e + comp] = comp ? sx * ik2 : -sy * ik2;
+        }
+      }
+    };
+    if (SPARSE) band_solve_v_sparse(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    else band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+  }
+}
+
+
+int modes_pair_count();
+const char *modes_pair_name(int v);
+void modes_pair_launch(int v, const ModeArgs &a, cudaStream_t st);
+void modes_dense_launch(const ModeArgs &a, cudaStream_t st);
+int modes_quad_count();
+const char *modes_quad_name(int v);
+void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st);
+
+}  // namespace owt

@@ -15,6 +15,7 @@
 
 #include "owt_device.cuh"
 #include "solve_kernels.h"
+#include "modes_kernel.cuh"
 
 namespace owt {
 
@@ -105,157 +106,17 @@ bool band_supported(int kl, int ku) {
   return (kl == 18 && ku == 15) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
 }
 
-// ---------------------------------------------------------------------------
-// Mode kernel: two threads per Fourier mode (one per real component).  For
-// mode (kz, kx):
-//  1. source_g = sum beta Hg_l + sum alpha g_l / dt      (solver.cpp:573-574)
-//  2. omega_y-system: g and DY1 g                         (solver.cpp:578, 603)
-//  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
-//     with DY2 v_l kept as a history of its own (q_l)    (solver.cpp:569-571)
-//  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
-//  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
-// ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG, bool SPARSE>
-__global__ void __launch_bounds__(128) k_modes(ModeArgs a) {
-  // Two threads per mode, one per real component (the band systems are real):
-  // lane 2m handles Re, lane 2m+1 Im; the pair's factor loads coincide.
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = tid >> 1, comp = tid & 1;
-  if (m >= a.M) return;
-  const int M = a.M, NY = a.NY;
-  const int k = m / a.NXH, i = m - k * a.NXH;
-  const int kabs = (k <= a.NZH) ? k : a.NZ - k;
-  const int u = kabs * a.NXH + i;
-  const double kx = a.kx[i], kz = a.kz[k];
-  const double k2 = kx * kx + kz * kz;
-  const long long s = *a.step;
-  const int h = ring_head(s);
-  const size_t fs2 = 2 * (size_t)NY * M;  // doubles per field
-  auto lvl = [&](const double2 *ring, int l) {
-    return reinterpret_cast<const double *>(ring) + (size_t)((h + l) % 3) * fs2 + comp;
-  };
-  const double *v0 = lvl(a.v_ring, 0), *v1 = lvl(a.v_ring, 1), *v2 = lvl(a.v_ring, 2);
-  const double *g0 = lvl(a.g_ring, 0), *g1 = lvl(a.g_ring, 1), *g2 = lvl(a.g_ring, 2);
-  const double *hv0 = lvl(a.hv_ring, 0), *hv1 = lvl(a.hv_ring, 1), *hv2 = lvl(a.hv_ring, 2);
-  const double *hg0 = lvl(a.hg_ring, 0), *hg1 = lvl(a.hg_ring, 1), *hg2 = lvl(a.hg_ring, 2);
-  const double *q0 = lvl(a.q_ring, 0), *q1 = lvl(a.q_ring, 1), *q2 = lvl(a.q_ring, 2);
-  const int hn = (h + 2) % 3;  // slot of the new level 0
-  double *vn = reinterpret_cast<double *>(a.v_ring) + (size_t)hn * fs2 + comp;
-  double *gn = reinterpret_cast<double *>(a.g_ring) + (size_t)hn * fs2 + comp;
-  double *qn = reinterpret_cast<double *>(a.q_ring) + (size_t)hn * fs2 + comp;
-  double *sg = reinterpret_cast<double *>(a.sg) + comp;
-  double *dg = reinterpret_cast<double *>(a.dg) + comp;
-  double *yv = reinterpret_cast<double *>(a.yv) + comp;
-  double *yg = reinterpret_cast<double *>(a.yg) + comp;
-  auto E = [&](int j) { return 2 * ((size_t)j * M + m); };  // offset of (j, m) in doubles
-  const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
-  const double idt = a.inv_dt;
-
-  // 1. source_g, walls zero (solver.cpp:573-574, 598-599)
-  for (int j = 0; j < NY; ++j) {
-    const size_t e = E(j);
-    double r = 0.0;
-    if (j != 0 && j != NY - 1)
-      r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
-    sg[e] = r;
-  }
-
-  // 2. omega_y-system: g and DY1 g
-  const double icg = a.inv_cg[u];
-  {
-    double d2 = 0.0;
-    auto rhs = [&](int p) -> double {
-      double acc = 0.0;
-#pragma unroll
-      for (int q = 0; q < 5; ++q) acc += a.rb_val[p * 5 + q] * sg[E(a.rb_col[p * 5 + q])];
-      return acc * (icg * a.rs_g[(size_t)p * a.U + u]);
-    };
-    auto ys = [&](int p, double y) { yg[E(p)] = y; };
-    auto yl = [&](int p) -> double { return yg[E(p)]; };
-    auto out = [&](int c, double x) {
-      const int jn = c >> 1;
-      if (c & 1) {
-        d2 = x * a.inv_h2;
-      } else {
-        x *= a.inv_h;
-        const size_t e = E(jn);
-        double g = 0.0;
-        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nu * a.c21[jn] * x + a.nu * a.c22[jn] * d2) * icg;
-        gn[e] = g;
-        dg[e] = a.c11[jn] * x;
-      }
-    };
-    band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
-  }
-  __syncwarp(__activemask());  // the partner's g, DY1 g are read below
-
-  // 3-5. v-system, then solve_horizontal's components
-  {
-    const double k2dt = k2 * idt;
-    const bool horiz = !(k2 < 1.e-8);
-    const double ik2 = horiz ? 1.0 / k2 : 0.0;
-    const double ax = kx * ik2, az = kz * ik2;
-    const double kzk2 = kz * k2, kxk2 = kx * k2;
-    double d1 = 0.0, d2 = 0.0;
-    auto rhs = [&](int p) -> double {
-      const int j = a.rhs_node_v[p];
-      if (j < 0) return 0.0;
-      const size_t e = E(j);
-      const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
-      const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
-      const double r = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
-      return r * a.rs_v[(size_t)p * a.U + u];
-    };
-    auto ys = [&](int p, double y) { yv[E(p)] = y; };
-    auto yl = [&](int p) -> double { return yv[E(p)]; };
-    auto out = [&](int c, double x) {
-      const int jn = c / 5, t = c - 5 * jn;
-      if (t == 2) {
-        d2 = x * a.inv_h2;
-      } else if (t == 1) {
-        d1 = x * a.inv_h;
-      } else if (t == 0) {
-        const size_t e = E(jn);
-        vn[e] = x;
-        const double q = a.c21[jn] * d1 + a.c22[jn] * d2;
-        qn[e] = q;
-        if (horiz) {
-          const double dv = a.c11[jn] * d1;
-          const unsigned mask = __activemask();
-          const double xo = __shfl_xor_sync(mask, x, 1), dvo = __shfl_xor_sync(mask, dv, 1),
-                       qo = __shfl_xor_sync(mask, q, 1);
-          // full complex values (re, im) of v, DY1 v, DY2 v, g, DY1 g
-          const double vr = comp ? xo : x, vi = comp ? x : xo;
-          const double dvr = comp ? dvo : dv, dvi = comp ? dv : dvo;
-          const double qr = comp ? qo : q, qi = comp ? q : qo;
-          const double *gp = gn - comp, *dgp = dg - comp;
-          const double gr = gp[e], gi = gp[e + 1], dgr = dgp[e], dgi = dgp[e + 1];
-          // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
-          // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
-          const double ur = -ax * dvi + az * gi, ui = ax * dvr - az * gr;
-          const double wr = -ax * gi - az * dvi, wi = ax * gr + az * dvr;
-          const double tx = kx * dgr + kz * qr - kzk2 * vr, ty = kx * dgi + kz * qi - kzk2 * vi;
-          const double sx = kz * dgr - kx * qr + kxk2 * vr, sy = kz * dgi - kx * qi + kxk2 * vi;
-          double *uo = reinterpret_cast<double *>(a.u_out), *wo = reinterpret_cast<double *>(a.w_out);
-          double *oxo = reinterpret_cast<double *>(a.ox_out), *ozo = reinterpret_cast<double *>(a.oz_out);
-          uo[e + comp] = comp ? ui : ur;
-          wo[e + comp] = comp ? wi : wr;
-          oxo[e + comp] = comp ? tx * ik2 : -ty * ik2;
-          ozo[e + comp] = comp ? sx * ik2 : -sy * ik2;
-        }
-      }
-    };
-    if (SPARSE) band_solve_v_sparse(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
-    else band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
-  }
+// Mode-kernel variants live in modes_pair.cu and modes_quad.cu (separate
+// translation units so they compile in parallel); this dispatches by index.
+int modes_variant_count() { return modes_pair_count() + modes_quad_count(); }
+const char *modes_variant_name(int v) {
+  return v < modes_pair_count() ? modes_pair_name(v) : modes_quad_name(v - modes_pair_count());
 }
-
-void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st) {
-  const int bs = 128, gs = (int)((2 * (long long)a.M + bs - 1) / bs);
-  if (klv == 18 && kuv == 15 && klg == 6 && kug == 6) {
-    if (sparse) k_modes<18, 15, 6, 6, true><<<gs, bs, 0, st>>>(a);
-    else k_modes<18, 15, 6, 6, false><<<gs, bs, 0, st>>>(a);
-  }
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st) {
+  if (!(klv == 18 && kuv == 15 && klg == 6 && kug == 6)) return;
+  if (!sparse) { modes_dense_launch(a, st); return; }
+  if (variant < modes_pair_count()) modes_pair_launch(variant, a, st);
+  else modes_quad_launch(variant - modes_pair_count(), a, st);
 }
 
 // Every factored v-system must keep its interior fill inside the masks: count
@@ -308,47 +169,60 @@ __global__ void k_mean(MeanArgs a) {
   const double *rs = a.rs_g;
   int stride = a.U;
   double2 *scr = a.scratch;
+  const int *rbc = a.rb_col;
+  const double *rbv = a.rb_val, *c11 = a.c11, *c21 = a.c21, *c22 = a.c22;
   if (SMEM) {
     double2 *ssc = reinterpret_cast<double2 *>(smraw);             // 2 NY + 2 n
     double *sab = reinterpret_cast<double *>(ssc + 2 * NY + 2 * n);  // NB n
     double *srs = sab + (size_t)NB * n;                             // n
-    uint8_t *spv = reinterpret_cast<uint8_t *>(srs + n);           // n
+    double *srbv = srs + n;                                         // 5 n
+    double *sc = srbv + 5 * (size_t)n;                              // 3 NY
+    int *srbc = reinterpret_cast<int *>(sc + 3 * (size_t)NY);       // 5 n
+    uint8_t *spv = reinterpret_cast<uint8_t *>(srbc + 5 * (size_t)n);  // n
     for (int e = t; e < NB * n; e += blockDim.x) sab[e] = a.ab_g[(size_t)e * a.U];
     for (int e = t; e < n; e += blockDim.x) {
       srs[e] = a.rs_g[(size_t)e * a.U];
       spv[e] = a.piv_g[(size_t)e * a.U];
     }
-    __syncthreads();
+    for (int e = t; e < 5 * n; e += blockDim.x) { srbv[e] = a.rb_val[e]; srbc[e] = a.rb_col[e]; }
+    for (int e = t; e < NY; e += blockDim.x) { sc[e] = a.c11[e]; sc[NY + e] = a.c21[e]; sc[2 * NY + e] = a.c22[e]; }
     ab = sab; piv = spv; rs = srs; stride = 1; scr = ssc;
+    rbc = srbc; rbv = srbv; c11 = sc; c21 = sc + NY; c22 = sc + 2 * NY;
   }
-  if (t < 2) {
-    double2 *U = (t == 0) ? a.U_ring : a.W_ring;
-    const double2 *L = (t == 0) ? a.lx_ring : a.lz_ring;
-    const double *F = (t == 0) ? a.fx_ring : a.fz_ring;
-    double2 *sg = scr + (size_t)t * NY;
-    double2 *yy = scr + 2 * (size_t)NY + (size_t)t * n;
-    double2 *dd = a.dy1 + (size_t)t * NY;
+  // right-hand sides of the U and W solves, all threads (solver.cpp:452-457)
+  {
     const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
-    const double f0 = F[o0], f1 = F[o1], f2 = F[o2];
-    for (int j = 0; j < NY; ++j) {
+    for (int e = t; e < 2 * NY; e += blockDim.x) {
+      const int q = e / NY, j = e - q * NY;
+      const double2 *U = q == 0 ? a.U_ring : a.W_ring;
+      const double2 *L = q == 0 ? a.lx_ring : a.lz_ring;
+      const double *F = q == 0 ? a.fx_ring : a.fz_ring;
       double2 r = make_double2(0.0, 0.0);
       if (j != 0 && j != NY - 1) {
+        const double f0 = F[o0], f1 = F[o1], f2 = F[o2];
         const double2 l0 = L[o0 * NY + j], l1 = L[o1 * NY + j], l2 = L[o2 * NY + j];
         const double2 u0 = U[o0 * NY + j], u1 = U[o1 * NY + j], u2 = U[o2 * NY + j];
         r.x = be0 * (l0.x + f0) + be1 * (l1.x + f1) + be2 * (l2.x + f2) +
               (al0 * u0.x + al1 * u1.x + al2 * u2.x) * a.inv_dt;
         r.y = be0 * l0.y + be1 * l1.y + be2 * l2.y + (al0 * u0.y + al1 * u1.y + al2 * u2.y) * a.inv_dt;
       }
-      sg[j] = r;
+      scr[(size_t)q * NY + j] = r;
     }
+  }
+  __syncthreads();
+  if (t < 2) {
+    double2 *U = (t == 0) ? a.U_ring : a.W_ring;
+    double2 *sg = scr + (size_t)t * NY;
+    double2 *yy = scr + 2 * (size_t)NY + (size_t)t * n;
+    double2 *dd = a.dy1 + (size_t)t * NY;
     const double icg = a.inv_cg0;
     double2 d2 = make_double2(0.0, 0.0);
     double2 *Un = U + (size_t)h * NY;
     auto rhs = [&](int p) -> double2 {
       double2 acc = make_double2(0.0, 0.0);
       for (int e = 0; e < 5; ++e) {
-        const double b = a.rb_val[p * 5 + e];
-        const double2 r = sg[a.rb_col[p * 5 + e]];
+        const double b = rbv[p * 5 + e];
+        const double2 r = sg[rbc[p * 5 + e]];
         acc.x += b * r.x;
         acc.y += b * r.y;
       }
@@ -366,13 +240,12 @@ __global__ void k_mean(MeanArgs a) {
         double2 g = make_double2(0.0, 0.0);
         if (jn != 0 && jn != NY - 1) {
           const double2 r = sg[jn];
-          const double w1 = a.nu * a.c21[jn], w2 = a.nu * a.c22[jn];
+          const double w1 = a.nu * c21[jn], w2 = a.nu * c22[jn];
           g.x = (r.x + w1 * x.x + w2 * d2.x) * icg;
           g.y = (r.y + w1 * x.y + w2 * d2.y) * icg;
         }
         Un[jn] = g;
-        const double c11 = a.c11[jn];
-        dd[jn] = make_double2(c11 * x.x, c11 * x.y);
+        dd[jn] = make_double2(c11[jn] * x.x, c11[jn] * x.y);
       }
     };
     band_solve<6, 6>(ab, piv, n, stride, 0, rhs, ys, yl, out);
@@ -398,7 +271,8 @@ __global__ void k_mean(MeanArgs a) {
 
 size_t mean_smem_bytes(int NY, int n_g) {
   return (2 * (size_t)NY + 2 * (size_t)n_g) * sizeof(double2) + 19 * (size_t)n_g * sizeof(double) +
-         (size_t)n_g * sizeof(double) + (size_t)n_g + 16;
+         (size_t)n_g * sizeof(double) + 5 * (size_t)n_g * (sizeof(double) + sizeof(int)) +
+         3 * (size_t)NY * sizeof(double) + (size_t)n_g + 16;
 }
 
 // Opt in to the shared memory of the staged mean-mode solve when it fits.
@@ -581,6 +455,58 @@ __global__ void k_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const doub
 void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
                             const long long *step, cudaStream_t st) {
   k_lamb_mean_shift<<<1, 256, 0, st>>>(lx_ring, lz_ring, lx, lz, NY, M, step);
+}
+
+// Wall-normal statistics by Parseval, one block per y plane, fixed reduction
+// order (deterministic).  Physical field f = sum_{kx>0} 2 Re(f_k e^{..}) +
+// Re(sum_kz f(0,kz) e^{..}) with the Nyquist kz row dropped, so the x-z mean of
+// f g is sum_{kx>0} 2 Re(f conj g) + sum_kz Re(Hf conj Hg) over the kx = 0
+// column's Hermitian parts Hf(kz) = (f(kz) + conj f(-kz))/2.
+__global__ void k_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out) {
+  const int j = blockIdx.x;
+  const int M = NZ * NXH, NZH = NZ / 2;
+  const double2 *pu = u + (size_t)j * M, *pv = v + (size_t)j * M, *pw = w + (size_t)j * M;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // uu, vv, ww, uv
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int k = m / NXH, i = m - k * NXH;
+    if (k == NZH) continue;
+    double2 a = pu[m], b = pv[m], c = pw[m];
+    double wgt = 2.0;
+    if (i == 0) {
+      const int kp = (k == 0) ? 0 : NZ - k;
+      const double2 ap = pu[(size_t)kp * NXH], bp = pv[(size_t)kp * NXH], cp = pw[(size_t)kp * NXH];
+      a = make_double2(0.5 * (a.x + ap.x), 0.5 * (a.y - ap.y));
+      b = make_double2(0.5 * (b.x + bp.x), 0.5 * (b.y - bp.y));
+      c = make_double2(0.5 * (c.x + cp.x), 0.5 * (c.y - cp.y));
+      wgt = 1.0;
+    }
+    acc[0] += wgt * (a.x * a.x + a.y * a.y);
+    acc[1] += wgt * (b.x * b.x + b.y * b.y);
+    acc[2] += wgt * (c.x * c.x + c.y * c.y);
+    acc[3] += wgt * (a.x * b.x + a.y * b.y);
+  }
+  __shared__ double red[4][256];
+  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double U = pu[0].x, V = pv[0].x, W = pw[0].x;
+    out[0 * NY + j] = U;
+    out[1 * NY + j] = V;
+    out[2 * NY + j] = W;
+    out[3 * NY + j] = sqrt(fmax(red[0][0] - U * U, 0.0));
+    out[4 * NY + j] = sqrt(fmax(red[1][0] - V * V, 0.0));
+    out[5 * NY + j] = sqrt(fmax(red[2][0] - W * W, 0.0));
+    out[6 * NY + j] = red[3][0] - U * V;
+  }
+}
+void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,
+                  cudaStream_t st) {
+  k_stats<<<NY, 256, 0, st>>>(u, v, w, NY, NZ, NXH, out);
 }
 
 // Reference layout [z][x][y] <-> device layout [y][z][x]: a transpose of an

@@ -98,7 +98,9 @@ bool band_supported(int kl, int ku);
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0, const double *t1,
                         const double *t2, const double *s1, const double *s2, double *rscale, int *info,
                         cudaStream_t st);
-void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, cudaStream_t st);
+void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
+int modes_variant_count();
+const char *modes_variant_name(int v);
 void launch_check_pattern(const double *ab, int n, int U, int *bad, cudaStream_t st);
 void launch_advance(long long *step, cudaStream_t st);
 void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st);
@@ -113,11 +115,14 @@ void launch_friction(const double2 *d1u, const double2 *d1w, const double *c11, 
 void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
                             const long long *step, cudaStream_t st);
 void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st);
+void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,
+                  cudaStream_t st);
 
 // Lamb vector: z-backward (6 fields) -> x pass with products -> z-forward (3).
 // precision 0: FP64, 1: FP32 transforms and products.  Returns launches issued.
 int launch_lamb(const XformArgs &a, int precision, cudaStream_t st);
 cudaError_t lamb_prepare(const XformDims &d);
+void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st);
 size_t lamb_zbuf_bytes(const XformDims &d, int precision);
 size_t lamb_lbuf_bytes(const XformDims &d, int precision);
 

@@ -141,30 +141,21 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   }
 }
 
-// Component f of Ubar x om(k) + u(k) x Obar at mode (kz, kx) and height j, in
-// FP64, where Ubar, Obar are the real parts of the (0, 0) modes (the mean flow
-// as the transforms see it) and the fields of the kx = 0 column enter through
-// their Hermitian part, as the real-part extraction of the x transform makes
-// them enter the physical product.  At (0, 0) it is Ubar x Obar.
-__device__ double2 mean_interaction(const XformArgs &a, int f, int j, int kz, int kx) {
-  const XformDims &d = a.d;
-  const int M = d.NZ * d.NXH;
-  const double2 *fld[6];
-  for (int q = 0; q < 6; ++q) {
-    const double2 *base = a.in[q];
-    if (a.ring_mask & (1 << q)) base += (size_t)ring_head(*a.step) * a.fs;
-    fld[q] = base + (size_t)j * M;
-  }
-  // mean vectors (u, v, w) and (ox, oy, oz): real parts of mode 0
-  double Ub[3], Ob[3];
-  for (int q = 0; q < 3; ++q) { Ub[q] = fld[q][0].x; Ob[q] = fld[3 + q][0].x; }
+// Component f of Ubar x om(k) + u(k) x Obar at mode (kz, kx), in FP64, where
+// Ubar, Obar are the real parts of the (0, 0) modes (the mean flow as the
+// transforms see it) and the fields of the kx = 0 column enter through their
+// Hermitian part, as the real-part extraction of the x transform makes them
+// enter the physical product.  At (0, 0) it is Ubar x Obar.  fld[q] points at
+// row j of field q; Ub, Ob hold the mean vectors of that row.
+__device__ __forceinline__ double2 mean_interaction(const double2 *const *fld, const double *Ub, const double *Ob,
+                                                    int NZ, int NXH, int f, int kz, int kx) {
   const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
   if (kz == 0 && kx == 0) return make_double2(Ub[f1] * Ob[f2] - Ub[f2] * Ob[f1], 0.0);
   auto val = [&](int q) -> double2 {
-    const double2 x = fld[q][(size_t)kz * d.NXH + kx];
+    const double2 x = fld[q][(size_t)kz * NXH + kx];
     if (kx != 0) return x;
-    const int kp = kz == 0 ? 0 : d.NZ - kz;
-    const double2 y = fld[q][(size_t)kp * d.NXH];
+    const int kp = kz == 0 ? 0 : NZ - kz;
+    const double2 y = fld[q][(size_t)kp * NXH];
     return make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
   };
   // (a x b)_f = a_f1 b_f2 - a_f2 b_f1
@@ -191,6 +182,18 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
   const cpx<T> *r = fft_lines<T, false>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
   const double sc = a.inv_nz2;
+  const double2 *fld[6];
+  double Ub[3], Ob[3];
+  if (a.mean_split) {
+    const int hd = ring_head(*a.step);
+    const size_t row = (size_t)j * d.NZ * d.NXH;
+    for (int q = 0; q < 6; ++q) {
+      const double2 *base = a.in[q];
+      if (a.ring_mask & (1 << q)) base += (size_t)hd * a.fs;
+      fld[q] = base + row;
+    }
+    for (int q = 0; q < 3; ++q) { Ub[q] = fld[q][0].x; Ob[q] = fld[3 + q][0].x; }
+  }
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
     const int kz = idx / TX, c = idx - kz * TX;
     if (i0 + c < d.NXH) {
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
       const double2 v = to_d(r[c * ls + slot]);
       double2 o = make_double2(v.x * sc, v.y * sc);
       if (a.mean_split && kz != d.NZH) {
-        const double2 l = mean_interaction(a, f, j, kz, i0 + c);
+        const double2 l = mean_interaction(fld, Ub, Ob, d.NZ, d.NXH, f, kz, i0 + c);
         o.x += l.x;
         o.y += l.y;
       }
@@ -244,6 +247,27 @@ cudaError_t lamb_prepare(const XformDims &d) {
 
 int launch_lamb(const XformArgs &a, int precision, cudaStream_t st) {
   return precision == 0 ? lamb_t<double>(a, st) : lamb_t<float>(a, st);
+}
+
+// One of the three kernels alone (0: z backward, 1: x pass, 2: z forward),
+// for timing.
+template <typename T>
+static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
+  const XformDims &d = a.d;
+  constexpr int TX = XCfg<T>::TX, P = XCfg<T>::P;
+  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  if (part == 0) {
+    k_zback<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), d.NZ2, sz, st>>>(a);
+  } else if (part == 1) {
+    const size_t nl = (size_t)d.NY * d.NZ2;
+    k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
+  } else {
+    k_zfwd<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
+  }
+}
+void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st) {
+  if (precision == 0) lamb_part_t<double>(a, part, st);
+  else lamb_part_t<float>(a, part, st);
 }
 
 size_t lamb_zbuf_bytes(const XformDims &d, int precision) {

@@ -72,6 +72,16 @@ def load(path=LIB):
         "owt_enqueue_stage": ([_h, C.c_int], C.c_int),
         "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),
         "owt_get_info": ([_h, C.c_int, C.POINTER(C.c_int64)], C.c_int),
+        "owt_tuning_report": ([_h], C.c_char_p),
+        "owt_statistics": ([_h, _dp], C.c_int),
+        "owt_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+        "owt_batch_step": ([C.c_void_p, C.c_int64], C.c_int),
+        "owt_batch_synchronize": ([C.c_void_p], C.c_int),
+        "owt_batch_destroy": ([C.c_void_p], C.c_int),
+        "owt_batch_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+        "owt_checkpoint_bytes": ([_h, C.POINTER(C.c_int64)], C.c_int),
+        "owt_checkpoint_save": ([_h, C.c_void_p, C.c_int64], C.c_int),
+        "owt_checkpoint_load": ([_h, C.c_void_p, C.c_int64], C.c_int),
         "owt_dy1_noalloc": ([C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     }
     for name, (args, res) in sig.items():

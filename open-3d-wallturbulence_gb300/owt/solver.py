@@ -132,6 +132,32 @@ class GpuSolver:
         self._chk(self.L.owt_get_grid(self.h, _L.dptr(y)))
         return y
 
+    STAT_NAMES = ("U", "V", "W", "u_rms", "v_rms", "w_rms", "uv")
+
+    def statistics(self):
+        """Wall-normal profiles of the current velocity (dict of NY arrays)."""
+        out = np.empty(7 * self.params.NY)
+        self._chk(self.L.owt_statistics(self.h, _L.dptr(out)))
+        return {n: out[q * self.params.NY:(q + 1) * self.params.NY].copy() for q, n in enumerate(self.STAT_NAMES)}
+
+    def checkpoint(self):
+        """The full state as bytes (exact restart)."""
+        n = C.c_int64()
+        self._chk(self.L.owt_checkpoint_bytes(self.h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        self._chk(self.L.owt_checkpoint_save(self.h, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf
+
+    def restore(self, image):
+        buf = np.ascontiguousarray(image, dtype=np.uint8)
+        self._chk(self.L.owt_checkpoint_load(self.h, buf.ctypes.data_as(C.c_void_p), buf.size))
+
+    def save_checkpoint(self, path):
+        self.checkpoint().tofile(path)
+
+    def load_checkpoint(self, path):
+        self.restore(np.fromfile(path, dtype=np.uint8))
+
     def enqueue_stage(self, stage):
         """Enqueue one stage (0 modes, 1 mean, 2 transforms, 3 nonlinear) for timing."""
         self._chk(self.L.owt_enqueue_stage(self.h, int(stage)))
@@ -139,8 +165,16 @@ class GpuSolver:
     def force_dense_bands(self, on=True):
         self._chk(self.L.owt_set_option(self.h, 1, 1 if on else 0))
 
+    def force_modes_variant(self, v):
+        """Run mode-kernel variant v (-1: the autotuned one)."""
+        self._chk(self.L.owt_set_option(self.h, 2, int(v)))
+
+    def tuning_report(self):
+        return self.L.owt_tuning_report(self.h).decode()
+
     def info(self, what):
-        codes = {"sparse_solve": 1, "pattern_violations": 2, "device_bytes": 3}
+        codes = {"sparse_solve": 1, "pattern_violations": 2, "device_bytes": 3, "modes_variant": 4,
+                 "modes_variants": 5}
         v = C.c_int64()
         self._chk(self.L.owt_get_info(self.h, codes[what], C.byref(v)))
         return v.value

@@ -205,6 +205,29 @@ def test_sparse_interior_solve_equals_full_band(gpu_lib):
         np.testing.assert_array_equal(a.get(n), b.get(n))
 
 
+def test_mode_kernel_variants_are_bitwise_equal(gpu_lib):
+    """The autotuner's candidates differ in thread mapping and block shape
+    only; every one gives the same bits."""
+    from owt.params import channel_180
+    from owt.ic import seeded_velocity
+    p = channel_180()
+    u, v, w = seeded_velocity(p, seed=3)
+    s = gpu_solver(p)
+    print("autotuner:", s.tuning_report())
+    ref = None
+    for var in range(s.info("modes_variants")):
+        s.force_modes_variant(var)
+        assert s.info("modes_variant") == var
+        s.init_fields(u, v, w)
+        s.time_Integration(2)
+        got = [s.get(n) for n in ("vely", "vory", "velx", "vorz", "Hv")]
+        if ref is None:
+            ref = got
+        else:
+            for a, b in zip(got, ref):
+                np.testing.assert_array_equal(a, b)
+
+
 def test_graph_replay_is_bitwise_equal_to_eager(gpu_lib, small):
     p, (u, v, w) = small
     a, b = gpu_solver(p), gpu_solver(p)

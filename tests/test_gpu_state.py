@@ -1,0 +1,97 @@
+"""Statistics, exact restart and snapshots on the GPU state."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["velx", "vely", "velz", "vorx", "vory", "vorz", "lmbx", "lmby", "lmbz", "Hv", "Hg",
+          "vely_0", "vely_1", "vely_2", "vory_0", "vory_1", "vory_2", "Hv_0", "Hv_1", "Hv_2", "Hg_0", "Hg_1", "Hg_2"]
+
+
+@pytest.fixture
+def run():
+    from owt.params import CaseParams
+    from owt.ic import seeded_velocity
+    from owt.solver import GpuSolver
+    p = CaseParams(dt=0.005, dkx=0.5, dkz=1.5, NX=32, NY=33, NZ=24, alpha_mesh=2.0, nu=1 / 2800.)
+    s = GpuSolver(p)
+    s.init_fields(*seeded_velocity(p, seed=4))
+    return p, s
+
+
+def test_statistics_match_host_parseval(gpu_lib, run):
+    from owt.snapshot import statistics_from_fields
+    p, s = run
+    s.time_Integration(3)
+    got = s.statistics()
+    want = statistics_from_fields(s.get("velx"), s.get("vely"), s.get("velz"), p.NZH)
+    for k in want:
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-12, atol=1e-14 * max(1.0, np.abs(want[k]).max()))
+    assert got["u_rms"].max() > 0.01 and abs(got["U"].max() - 1.5) < 0.1
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_restart_from_checkpoint_is_bitwise(gpu_lib, run, graph):
+    p, s = run
+    s.use_graph(graph)
+    s.time_Integration(4)        # ring head not at its start value
+    image = s.checkpoint()
+    s.time_Integration(3)
+    a = {n: s.get(n) for n in FIELDS}
+    fa = s.friction()
+    s.restore(image)
+    assert s.step == 4
+    s.time_Integration(3)
+    for n in FIELDS:
+        np.testing.assert_array_equal(s.get(n), a[n], err_msg=n)
+    np.testing.assert_array_equal(s.friction(), fa)
+
+
+def test_checkpoint_rejects_other_parameters(gpu_lib, run):
+    from owt.lib import OwtError
+    from owt.params import CaseParams
+    from owt.solver import GpuSolver
+    p, s = run
+    img = s.checkpoint()
+    q = CaseParams(dt=0.004, dkx=0.5, dkz=1.5, NX=32, NY=33, NZ=24, alpha_mesh=2.0, nu=1 / 2800.)
+    t = GpuSolver(q)
+    with pytest.raises(OwtError):
+        t.restore(img)
+
+
+def test_snapshot_round_trip(gpu_lib, run, tmp_path):
+    from owt.snapshot import save_instant_field, load_instant_field
+    p, s = run
+    s.time_Integration(2)
+    path = save_instant_field(s, 2, directory=str(tmp_path / "DATA"))
+    assert path.endswith("F-00000002.npz")
+    d = load_instant_field(path)
+    for n in ("velx", "vely", "velz"):
+        np.testing.assert_array_equal(d[n], s.get(n))
+        assert d[n].shape == (p.NZ, p.NXH, p.NY)
+
+
+def test_batch_step_matches_individual_steps(gpu_lib):
+    """Channels of uneven sizes stepped as one graph launch give the same bits
+    as stepping each alone."""
+    from owt.batch import minimal_channels, Batch
+    from owt.ic import seeded_velocity
+    from owt.solver import GpuSolver
+    ps = minimal_channels(4, seed=2)
+    alone, batched = [], []
+    for q, p in enumerate(ps):
+        for group in (alone, batched):
+            s = GpuSolver(p, precision="mixed")
+            s.init_fields(*seeded_velocity(p, seed=q))
+            group.append(s)
+    b = Batch(batched)
+    b.step(3)
+    b.synchronize()
+    for s in alone:
+        s.time_Integration(3)
+    for a, c in zip(alone, batched):
+        assert c.step == 3
+        for n in ("vely", "vory", "velx", "Hv", "lmbz"):
+            np.testing.assert_array_equal(a.get(n), c.get(n))
+        np.testing.assert_array_equal(a.friction(), c.friction())
+    b.close()
