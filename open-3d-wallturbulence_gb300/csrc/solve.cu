@@ -279,7 +279,7 @@ size_t mean_smem_bytes(int NY, int n_g) {
 bool mean_prepare(int NY, int n_g) {
   const size_t b = mean_smem_bytes(NY, n_g);
   if (b > 200 * 1024) return false;
-  return cudaFuncSetAttribute(k_mean<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b) == cudaSuccess;
+  return raise_smem_limit(k_mean<true>, b) == cudaSuccess;
 }
 
 void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st) {

@@ -4,9 +4,29 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "owt_device.cuh"
 
 namespace owt {
+
+// The dynamic shared-memory limit is an attribute of the kernel function on
+// the current device, shared by every handle of the process.  Raise it to
+// what a handle needs, never lower it: a smaller channel created after a
+// larger one must not break the larger one's launches.
+inline std::mutex &smem_attr_mutex() {
+  static std::mutex mu;
+  return mu;
+}
+template <typename F>
+inline cudaError_t raise_smem_limit(F *func, size_t bytes) {
+  std::lock_guard<std::mutex> lk(smem_attr_mutex());
+  cudaFuncAttributes at;
+  cudaError_t e = cudaFuncGetAttributes(&at, func);
+  if (e != cudaSuccess) return e;
+  if ((size_t)at.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
 
 struct ModeArgs {
   int NY, NZ, NXH, NZH, M, U;

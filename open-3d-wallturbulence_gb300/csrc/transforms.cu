@@ -232,9 +232,9 @@ static int lamb_t(const XformArgs &a, cudaStream_t st) {
 template <typename T>
 static cudaError_t prepare_t(const XformDims &d) {
   const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
-  cudaError_t e = cudaFuncSetAttribute(k_zback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_zfwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_xlamb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
+  cudaError_t e = raise_smem_limit(k_zback<T>, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k_zfwd<T>, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k_xlamb<T>, sx);
   return e;
 }
 

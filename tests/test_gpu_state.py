@@ -71,6 +71,31 @@ def test_snapshot_round_trip(gpu_lib, run, tmp_path):
         assert d[n].shape == (p.NZ, p.NXH, p.NY)
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_smaller_channel_created_later_leaves_larger_one_working(gpu_lib, graph):
+    """Kernel shared-memory limits are per function, not per handle: creating a
+    smaller channel after a larger one must not break the larger one's step."""
+    from owt.params import CaseParams
+    from owt.ic import seeded_velocity
+    from owt.solver import GpuSolver
+    big = CaseParams(dt=0.004, dkx=1.0, dkz=2.0, NX=96, NY=97, NZ=96, alpha_mesh=2.0, nu=1 / 3000.)
+    small = CaseParams(dt=0.004, dkx=1.0, dkz=2.0, NX=16, NY=17, NZ=16, alpha_mesh=2.0, nu=1 / 3000.)
+    ref = GpuSolver(big)
+    ref.use_graph(graph)
+    ref.init_fields(*seeded_velocity(big, seed=1))
+    ref.time_Integration(2)
+    want = ref.get("vely")
+    ref.close()
+    s = GpuSolver(big)
+    s.use_graph(graph)
+    s.init_fields(*seeded_velocity(big, seed=1))
+    t = GpuSolver(small)
+    t.init_fields(*seeded_velocity(small, seed=1))
+    t.time_Integration(1)
+    s.time_Integration(2)
+    np.testing.assert_array_equal(s.get("vely"), want)
+
+
 def test_batch_step_matches_individual_steps(gpu_lib):
     """Channels of uneven sizes stepped as one graph launch give the same bits
     as stepping each alone."""
