@@ -233,6 +233,36 @@ const char *owt_tuning_report(const owt_handle *h);
 #define OWT_STAGE_ZFWD 6
 int owt_enqueue_stage(owt_handle *h, int stage);
 
+/* Wall blowing/suction.  The reference imposes v = 0 on both walls through
+ * the boundary rows of the v-system (src/solver.cpp:581-596, source_v[0] and
+ * source_v[NY-1] set to zero); these calls put prescribed values there
+ * instead: v(y = -1) = vw_bottom, v(y = +1) = vw_top, each a spectral wall
+ * field of NZ * NX/2 complex128 values (interleaved re, im) in the layout of
+ * one y-line set of a Field, [kz index][kx index].  Mode (0, 0) should be zero
+ * (no net mass flux).  Both NULL restores no-slip.  get returns zeros when
+ * no wall velocity is set. */
+int owt_set_wall_velocity(owt_handle *h, const double *vw_bottom, const double *vw_top);
+int owt_get_wall_velocity(owt_handle *h, double *vw_bottom, double *vw_top);
+
+/* Wall-drag objective and its discrete adjoint (no counterpart in the
+ * reference).  J = (1/N) sum_{n=1..N} fx_n, the driving force fx of each of
+ * N steps (solve_friction_force, src/solver.cpp:306-312), which is the wall
+ * shear stress averaged over both walls.
+ *  - owt_drag_forward runs N steps from the current state (as
+ *    owt_time_integration would), keeping a device image of the full state
+ *    every `interval` steps, and returns J.  FP64 precision only.
+ *  - owt_drag_backward gives grad_objective * dJ/d(vw) for the wall velocity
+ *    in force during the forward run, as d/dRe + i d/dIm per mode, same
+ *    layout as owt_set_wall_velocity.  It recomputes each segment of
+ *    `interval` steps from its image and runs the adjoint step kernels
+ *    backwards through it; afterwards the state is again the state after the
+ *    forward run.  OWT_ERR_STATE if the state or the wall velocity changed
+ *    since owt_drag_forward.
+ * Device memory: (N/interval + 1) state images of ~15 fields each, a tape of
+ * 6 * interval fields, and ~45 fields of adjoint state and scratch. */
+int owt_drag_forward(owt_handle *h, int64_t nsteps, int64_t interval, double *objective);
+int owt_drag_backward(owt_handle *h, double grad_objective, double *grad_bottom, double *grad_top);
+
 /* DY1 along y for device arrays the caller owns, allocating no device memory.
  * No counterpart in the reference: it is the compact first derivative of
  * owt_dy_apply (order 1), out = diag(c11) A1^-1 B1 in, for callers that must

@@ -16,6 +16,7 @@ namespace owt {
 //  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
 //     with DY2 v_l kept as a history of its own (q_l)    (solver.cpp:569-571)
 //  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
+//     with v = v_w on the walls when blowing/suction is set
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
 // ---------------------------------------------------------------------------
 template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
@@ -118,7 +119,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
     double d1 = 0.0, d2 = 0.0;
     auto rhs = [&](int p) -> double {
       const int j = a.rhs_node_v[p];
-      if (j < 0) return 0.0;
+      if (j < 0) {
+        // wall rows: v = v_w (blowing/suction) or 0 (solver.cpp:593-596)
+        if (j == -1 || !a.vw) return 0.0;
+        const double *vw = reinterpret_cast<const double *>(a.vw) + (j == -2 ? 0 : 2 * (size_t)M);
+        return vw[2 * m + comp] * a.rs_v[(size_t)p * a.U + u];
+      }
       const size_t e = E(j);
       const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
       const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;

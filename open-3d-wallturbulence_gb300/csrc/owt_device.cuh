@@ -324,4 +324,78 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
   }
 }
 
+// ---------------------------------------------------------------------------
+// Transposed solve A^T x = b on the factors of band_solve (the order of LAPACK
+// dgbtrs with trans = 'T'): U^T y = b by forward substitution, then for
+// j = n-1 .. 0: b_j -= sum_i L(j+i, j) b_(j+i) and undo row interchange j.
+// Band entries outside the matrix are zero in the factorization layout, so
+// the rings start at zero and need no edge tests.
+//   rhs(p)      : entry p of b, requested for p = 0 .. n-1
+//   ystore/yload: scratch for y
+//   out(c, x)   : solution entry c, produced for c = n-1 .. 0
+// ---------------------------------------------------------------------------
+template <int KL, int KU, class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve_t(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
+                                             int U, int u, Rhs rhs, YStore ystore, YLoad yload, Out out) {
+  using V = decltype(rhs(0));
+  constexpr int KV = KL + KU;
+  const size_t sn = (size_t)n * U;
+  {
+    // y_j = (b_j - sum_t U(j-t, j) y_(j-t)) / U(j, j); y_(j-t) in slot (s - t) mod W
+    constexpr int W = KV + 1;
+    V w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = vzero<V>();
+    for (int j0 = 0; j0 < n; j0 += W) {
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int j = j0 + s;
+        if (j < n) {
+          const double *col = ab + (size_t)j * U + u;
+          V acc = rhs(j);
+#pragma unroll
+          for (int t = 1; t <= KV; ++t) fms(acc, col[(size_t)(KV - t) * sn], w[(s - t + W) % W]);
+          acc = scal(acc, col[(size_t)KV * sn]);
+          w[s] = acc;
+          ystore(j, acc);
+        }
+      }
+    }
+  }
+  {
+    // window b_j .. b_(j+KL): entry j + i in slot (s - i) mod W at the step of
+    // column j = n-1 - (jj + s); entry j + KL is final once column j is done
+    constexpr int W = KL + 1;
+    V w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = vzero<V>();
+    for (int jj = 0; jj < n + KL; jj += W) {
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int j = n - 1 - (jj + s);
+        if (j >= 0) {
+          const double *col = ab + (size_t)j * U + u;
+          V acc = yload(j);
+#pragma unroll
+          for (int i = 1; i <= KL; ++i) fms(acc, col[(size_t)(KV + i) * sn], w[(s - i + W) % W]);
+          w[s] = acc;
+          const int off = piv[(size_t)j * U + u];
+#pragma unroll
+          for (int i = 1; i <= KL; ++i) {
+            if (off == i) {
+              const V tmp = w[s];
+              w[s] = w[(s - i + W) % W];
+              w[(s - i + W) % W] = tmp;
+            }
+          }
+        } else {
+          w[s] = vzero<V>();
+        }
+        const int c = j + KL;
+        if (c >= 0 && c < n) out(c, w[(s + 1) % W]);
+      }
+    }
+  }
+}
+
 }  // namespace owt

@@ -236,6 +236,7 @@ BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu) {
     Eq e;
     if (j == 0 || j == N - 1) {
       e.add(V(j), 1.0);
+      e.rhs_node = j == 0 ? kRhsWallBottom : kRhsWallTop;
     } else if (j == 1) {
       e.add(D(1, 0), g.c11[0]);
     } else if (j == N - 2) {

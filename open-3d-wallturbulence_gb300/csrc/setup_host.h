@@ -60,6 +60,10 @@ struct Stencils {
   double b(int n, int i, int j) const { return B[n][(size_t)i * N + j]; }
 };
 
+// rhs_node tags of the two rows v_0 = v_w(bottom), v_N-1 = v_w(top); both are
+// zero (no-slip, src/solver.cpp:593-596) unless wall blowing/suction is set.
+constexpr int kRhsWallBottom = -2, kRhsWallTop = -3;
+
 // One equation: coefficients on unknown columns, split as
 // value(k) = t0 + s1(k) * t1 + s2(k) * t2 with per-mode scalars s1, s2.
 struct Entry {
@@ -74,7 +78,8 @@ struct BandTemplate {
   int per_node = 0;
   // [(kl+ku+1) x n]: entry (i, j) of the ordered matrix at row ku + i - j.
   std::vector<double> t0, t1, t2;
-  // v-system: for each row position, the node whose r feeds it (-1: zero rhs).
+  // v-system: for each row position, the node whose r feeds it (-1: zero rhs;
+  // kRhsWallBottom / kRhsWallTop: the wall-velocity rows v_0 and v_N-1).
   std::vector<int> rhs_node;
   // omega_y-system: rhs of row p = (1/cg) sum_e rb_val[p][e] * r[rb_col[p][e]].
   std::vector<int> rb_col;     // [n x 5]

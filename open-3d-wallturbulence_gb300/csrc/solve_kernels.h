@@ -43,6 +43,7 @@ struct ModeArgs {
   double inv_h, inv_h2;       // unscaling of solved h d1, h^2 d2
   double2 *sg, *dg, *yv, *yg;  // scratch
   const long long *step;
+  const double2 *vw;  // wall-normal velocity at the walls [2][M] (bottom, top), or null
 };
 
 struct MeanArgs {

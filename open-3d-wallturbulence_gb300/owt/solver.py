@@ -179,6 +179,41 @@ class GpuSolver:
         self._chk(self.L.owt_get_info(self.h, codes[what], C.byref(v)))
         return v.value
 
+    # -- wall blowing/suction and the wall-drag adjoint ----------------------------
+    def set_wall_velocity(self, bottom, top):
+        """v on the walls as spectral wall fields [NZ, NX/2] complex (None, None: no-slip)."""
+        if bottom is None and top is None:
+            self._chk(self.L.owt_set_wall_velocity(self.h, None, None))
+            return
+        shp = self.shape[:2]
+        b = np.ascontiguousarray(bottom, dtype=np.complex128)
+        t = np.ascontiguousarray(top, dtype=np.complex128)
+        if b.shape != shp or t.shape != shp:
+            raise ValueError(f"wall fields must have shape {shp}")
+        self._chk(self.L.owt_set_wall_velocity(self.h, _L.dptr(b.view(np.float64)), _L.dptr(t.view(np.float64))))
+
+    def wall_velocity(self):
+        shp = self.shape[:2]
+        b = np.empty(shp, np.complex128)
+        t = np.empty(shp, np.complex128)
+        self._chk(self.L.owt_get_wall_velocity(self.h, _L.dptr(b.view(np.float64)), _L.dptr(t.view(np.float64))))
+        return b, t
+
+    def drag_forward(self, nsteps, interval=20):
+        """Run nsteps steps; returns J = mean over the steps of the driving force fx."""
+        J = C.c_double()
+        self._chk(self.L.owt_drag_forward(self.h, int(nsteps), int(interval), C.byref(J)))
+        return J.value
+
+    def drag_backward(self, grad_objective=1.0):
+        """dJ/d(wall velocity) of the last drag_forward, as (bottom, top) [NZ, NX/2] complex."""
+        shp = self.shape[:2]
+        b = np.empty(shp, np.complex128)
+        t = np.empty(shp, np.complex128)
+        self._chk(self.L.owt_drag_backward(self.h, float(grad_objective), _L.dptr(b.view(np.float64)),
+                                           _L.dptr(t.view(np.float64))))
+        return b, t
+
     def set_precision(self, precision):
         self._chk(self.L.owt_set_precision(self.h, _L.PREC[precision]))
 

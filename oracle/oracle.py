@@ -170,6 +170,17 @@ class PortOracle(_Common):
         self.lib.port_time_modes.restype = C.c_double
         self.lib.port_time_transforms.argtypes = [C.c_long]
         self.lib.port_time_transforms.restype = C.c_double
+        self.lib.port_set_wall_velocity.argtypes = [_dp, _dp]
+        self.lib.port_set_wall_velocity.restype = C.c_int
+
+    def set_wall_velocity(self, bottom, top):
+        """Wall blowing/suction [NZ, NX/2] complex per wall; None, None: no-slip."""
+        if bottom is None:
+            self._chk(self.lib.port_set_wall_velocity(None, None), "set_wall_velocity")
+            return
+        b = np.ascontiguousarray(bottom, dtype=np.complex128).reshape(-1).view(np.float64)
+        t = np.ascontiguousarray(top, dtype=np.complex128).reshape(-1).view(np.float64)
+        self._chk(self.lib.port_set_wall_velocity(_ptr(b), _ptr(t)), "set_wall_velocity")
 
     def set_threads(self, n):
         return self.lib.port_set_threads(int(n))

@@ -20,7 +20,9 @@
 //   start-up sequence .............. src/solver.cpp:379-425
 //   solve_mean ..................... src/solver.cpp:428-514
 //   solve_horizontal ............... src/solver.cpp:516-539
-//   time_Integration ............... src/solver.cpp:541-627
+//   time_Integration ............... src/solver.cpp:541-627 (optionally with
+//                                    wall blowing/suction values in the v
+//                                    boundary rows, :593-596)
 //   Fourier2Physical_dealiased ..... src/FFT.cpp:49-128
 //   Physical2Fourier_dealiased ..... src/FFT.cpp:130-194
 //   dense mat-vec (j outer) ........ src/linalg.hpp:434-453
@@ -229,6 +231,9 @@ struct Port {
   std::map<std::string, std::vector<cplx>> V;  // mean-mode vectors
   std::map<std::string, double> S;
   CpuFft fzb, fzf, fxb, fxf;
+  // wall blowing/suction [z][x]: the values the v boundary rows take in place
+  // of the reference's zeros (solver.cpp:593-596); empty = no-slip
+  std::vector<cplx> vw_bot, vw_top;
 
   size_t nfield() const { return (size_t)NZ * NXH * NY; }
   cplx *f(const std::string &n) { return F.at(n).data(); }
@@ -552,6 +557,7 @@ struct Port {
         }
         Av(0, 0) = 1.0; Av(N - 1, N - 1) = 1.0; Ag(0, 0) = 1.0; Ag(N - 1, N - 1) = 1.0;
         sv[0] = 0.0; sv[1] = 0.0; sv[N - 2] = 0.0; sv[N - 1] = 0.0;
+        if (!vw_bot.empty()) { sv[0] = vw_bot[m]; sv[N - 1] = vw_top[m]; }
         sg[0] = 0.0; sg[N - 1] = 0.0;
         lu_factor(Av, pv);
         lu_solve(Av, pv, sv.data());
@@ -665,6 +671,14 @@ int port_call(const char *name) {
     else if (s == "solve_friction_force") g_port.solve_friction_force();
     else if (s == "time_Integration") g_port.time_integration();
     else throw std::invalid_argument(s);
+  });
+}
+int port_set_wall_velocity(const double *bottom, const double *top) {
+  return guarded([&] {
+    const size_t n = (size_t)g_port.NZ * g_port.NXH;
+    if (!bottom || !top) { g_port.vw_bot.clear(); g_port.vw_top.clear(); return; }
+    g_port.vw_bot.assign(reinterpret_cast<const cplx *>(bottom), reinterpret_cast<const cplx *>(bottom) + n);
+    g_port.vw_top.assign(reinterpret_cast<const cplx *>(top), reinterpret_cast<const cplx *>(top) + n);
   });
 }
 int port_get_field(const char *name, double *out) {
