@@ -56,6 +56,12 @@ typedef struct owt_params {
   int64_t NX, NY, NZ; /* modes: NX/2 kx, NZ kz, NY wall-normal points */
   int32_t precision;  /* OWT_PREC_FP64 or OWT_PREC_MIXED */
   int32_t device;     /* CUDA device ordinal */
+  /* Interior order of the compact finite differences.  0 or 8: the
+   * reference's schemes (src/compdiff.hpp, 8th order for D1-D3, 6th for D4);
+   * 6: sixth-order tridiagonal interior schemes for D1-D3 (D4 and every
+   * boundary closure unchanged).  Zero-initialising the struct selects the
+   * reference's operators. */
+  int32_t fd_order;
 } owt_params;
 
 /* Spectral fields, the reference globals of the same names

@@ -150,6 +150,8 @@ struct owt_handle {
       throw OwtError(OWT_ERR_INVALID, "dt, nu, dkx, dkz and alpha_mesh must be positive");
     if (p.precision != OWT_PREC_FP64 && p.precision != OWT_PREC_MIXED)
       throw OwtError(OWT_ERR_INVALID, "precision must be OWT_PREC_FP64 or OWT_PREC_MIXED");
+    if (p.fd_order != 0 && p.fd_order != 6 && p.fd_order != 8)
+      throw OwtError(OWT_ERR_INVALID, "fd_order must be 0 or 8 (the reference's schemes) or 6");
     NXH = NX / 2; NZH = NZ / 2; NX2 = NX / 2 * 3; NZ2 = NZ / 2 * 3;
     M = NZ * NXH;
     Uq = NXH * (NZH + 1);
@@ -170,11 +172,14 @@ struct owt_handle {
     // grid, metric, stencils, band templates (host, FP64)
     grid = make_grid(NY, p.alpha_mesh);
     Ly = grid.y[NY - 1] - grid.y[0];
-    Stencils sten = make_stencils(NY, grid.ds);
+    Stencils sten = make_stencils(NY, grid.ds, p.fd_order == 6 ? 6 : 8);
     BandTemplate tv = build_v_system(grid, sten, p.nu);
     BandTemplate tg = build_g_system(grid, sten, p.nu);
     BandTemplate t1 = build_plain_band(sten, 0);
     BandTemplate t2 = build_plain_band(sten, 1);
+    // the kernels are specialised for the bands of the reference's stencils
+    pad_band(tv, 18, 15);
+    pad_band(tg, 6, 6);
     for (const BandTemplate *t : {&tv, &tg, &t1, &t2})
       if (!band_supported(t->kl, t->ku))
         throw OwtError(OWT_ERR_INVALID, "unsupported band width " + std::to_string(t->kl) + "/" + std::to_string(t->ku));

@@ -48,8 +48,10 @@ Grid make_grid(int N, double alpha) {
   return g;
 }
 
-Stencils make_stencils(int N, double h) {
+Stencils make_stencils(int N, double h, int order) {
   if (N < 7) throw std::invalid_argument("NY must be at least 7 for the 3rd-derivative scheme");
+  if (order != 6 && order != 8) throw std::invalid_argument("compact-FD order must be 6 or 8");
+  const bool six = order == 6;
   Stencils st;
   st.N = N;
   for (int q = 0; q < 4; ++q) {
@@ -60,7 +62,9 @@ Stencils make_stencils(int N, double h) {
   auto B = [&](int q, int i, int j) -> double & { return st.B[q][(size_t)i * N + j]; };
   // First derivative, src/compdiff.hpp:11-69.
   {
-    const double al = 4.0 / 9.0, be = 1.0 / 36.0, a = 40.0 / 27.0, b = 25.0 / 54.0;
+    // sixth order: alpha 1/3, a 14/9, b 1/9 (tridiagonal)
+    const double al = six ? 1.0 / 3.0 : 4.0 / 9.0, be = six ? 0.0 : 1.0 / 36.0;
+    const double a = six ? 14.0 / 9.0 : 40.0 / 27.0, b = six ? 1.0 / 9.0 : 25.0 / 54.0;
     for (int i = 2; i < N - 2; ++i) {
       A(0, i, i - 2) = be; A(0, i, i - 1) = al; A(0, i, i) = 1.0; A(0, i, i + 1) = al; A(0, i, i + 2) = be;
       B(0, i, i - 2) = -b / (4 * h); B(0, i, i - 1) = -a / (2 * h); B(0, i, i + 1) = a / (2 * h);
@@ -80,8 +84,13 @@ Stencils make_stencils(int N, double h) {
   // the top row's (N-1, N-4) entry is 0 and (N-1, N-5) is never set).
   {
     const double h2 = std::pow(h, 2);
-    const double al = 344.0 / 1179.0, be = 23.0 / 2358.0, a = 320.0 / 393.0, b = 310.0 / 393.0;
+    // sixth order: alpha 2/11, a 12/11, b 3/11 (tridiagonal) on rows 3..N-4;
+    // rows 2, N-3 keep the reference's scheme, since rows 1, N-2 below are the
+    // sixth-order scheme centred on nodes 2, N-3 and must not repeat them
     for (int i = 2; i < N - 2; ++i) {
+      const bool s6 = six && i >= 3 && i <= N - 4;
+      const double al = s6 ? 2.0 / 11.0 : 344.0 / 1179.0, be = s6 ? 0.0 : 23.0 / 2358.0;
+      const double a = s6 ? 12.0 / 11.0 : 320.0 / 393.0, b = s6 ? 3.0 / 11.0 : 310.0 / 393.0;
       A(1, i, i - 2) = be; A(1, i, i - 1) = al; A(1, i, i) = 1.0; A(1, i, i + 1) = al; A(1, i, i + 2) = be;
       B(1, i, i - 2) = b / (4 * h2); B(1, i, i - 1) = a / h2; B(1, i, i) = -2 * b / (4 * h2) - 2 * a / h2;
       B(1, i, i + 1) = a / h2; B(1, i, i + 2) = b / (4 * h2);
@@ -103,7 +112,9 @@ Stencils make_stencils(int N, double h) {
   // does not annihilate constants; it is reproduced on purpose.
   {
     const double h3 = std::pow(h, 3);
-    const double al = 147.0 / 332.0, be = 1.0 / 166.0, a = 160.0 / 83.0, b = -5.0 / 166.0;
+    // sixth order: alpha 7/16, a 2, b -1/8 (tridiagonal)
+    const double al = six ? 7.0 / 16.0 : 147.0 / 332.0, be = six ? 0.0 : 1.0 / 166.0;
+    const double a = six ? 2.0 : 160.0 / 83.0, b = six ? -1.0 / 8.0 : -5.0 / 166.0;
     for (int i = 3; i < N - 3; ++i) {
       A(2, i, i - 2) = be; A(2, i, i - 1) = al; A(2, i, i) = 1.0; A(2, i, i + 1) = al; A(2, i, i + 2) = be;
       B(2, i, i - 3) = -b / (8 * h3); B(2, i, i - 2) = -a / (2 * h3); B(2, i, i - 1) = a / h3 + 3 * b / (8 * h3);
@@ -311,7 +322,21 @@ BandTemplate build_g_system(const Grid &g, const Stencils &st, double nu) {
   return bt;
 }
 
-BandTemplate build_plain_band(const Stencils &st, int which) {
+void pad_band(BandTemplate &bt, int kl, int ku) {
+  if (kl <= bt.kl && ku <= bt.ku) return;
+  const int nkl = std::max(kl, bt.kl), nku = std::max(ku, bt.ku), n = bt.n;
+  const int nb = nkl + nku + 1, shift = nku - bt.ku, ob = bt.kl + bt.ku + 1;
+  for (std::vector<double> *t : {&bt.t0, &bt.t1, &bt.t2}) {
+    std::vector<double> w((size_t)nb * n, 0.0);
+    for (int b = 0; b < ob; ++b)
+      for (int c = 0; c < n; ++c) w[(size_t)(b + shift) * n + c] = (*t)[(size_t)b * n + c];
+    t->swap(w);
+  }
+  bt.kl = nkl;
+  bt.ku = nku;
+}
+
+BandTemplate build_plain_band(const Stencils &st, int which, int min_kl, int min_ku) {
   const int N = st.N;
   BandTemplate bt;
   bt.n = N;
@@ -330,6 +355,7 @@ BandTemplate build_plain_band(const Stencils &st, int which) {
     for (int c = 0; c < N; ++c)
       if (st.a(which, i, c) != 0.0) bt.t0[(size_t)(bt.ku + i - c) * N + c] = st.a(which, i, c);
   bt.rhs_node.assign(N, -1);
+  pad_band(bt, min_kl, min_ku);
   return bt;
 }
 

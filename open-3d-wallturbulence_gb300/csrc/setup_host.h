@@ -87,11 +87,18 @@ struct BandTemplate {
 };
 
 Grid make_grid(int N, double alpha);
-Stencils make_stencils(int N, double h);
+// Compact-FD stencils; order 8 (the reference's interior schemes) or 6
+// (sixth-order tridiagonal interior schemes for D1-D3, same boundary rows).
+Stencils make_stencils(int N, double h, int order = 8);
 BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu);
 BandTemplate build_g_system(const Grid &g, const Stencils &st, double nu);
-// Band LU (no per-mode scalars) of A_1, shared by every mode for DY1 f.
-BandTemplate build_plain_band(const Stencils &st, int which);
+// Band LU (no per-mode scalars) of A_1, shared by every mode for DY1 f; the
+// band is at least (min_kl, min_ku) wide (zero diagonals pad narrower stencils).
+BandTemplate build_plain_band(const Stencils &st, int which, int min_kl = 2, int min_ku = 2);
+
+// Widen a band template to at least (kl, ku) with zero diagonals, so that a
+// narrower stencil set runs in the kernels specialised for the wider band.
+void pad_band(BandTemplate &bt, int kl, int ku);
 
 // Twiddle table exp(-2 pi i k / L), k in [0, L), interleaved (re, im).
 std::vector<double> twiddles(int L);

@@ -26,7 +26,7 @@ STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NUMERIC", 4: "STATE", 5: "NOMEM"
 class OwtParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("dkx", C.c_double), ("dkz", C.c_double), ("alpha_mesh", C.c_double),
                 ("nu", C.c_double), ("NX", C.c_int64), ("NY", C.c_int64), ("NZ", C.c_int64),
-                ("precision", C.c_int32), ("device", C.c_int32)]
+                ("precision", C.c_int32), ("device", C.c_int32), ("fd_order", C.c_int32)]
 
 
 class OwtError(RuntimeError):

@@ -28,6 +28,9 @@ class CaseParams:
     PZ: int = 1
     save_interval: int = 1
     extra: dict = field(default_factory=dict)
+    # interior compact-FD order: 8 = the reference's schemes, 6 = sixth-order
+    # tridiagonal interior schemes (not a reference toml key)
+    fd_order: int = 8
 
     @property
     def NXH(self):

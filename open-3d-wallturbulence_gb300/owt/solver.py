@@ -25,7 +25,7 @@ class GpuSolver:
         self.L = _L.load()
         self.params = params
         p = _L.OwtParams(params.dt, params.dkx, params.dkz, params.alpha_mesh, params.nu, params.NX, params.NY,
-                         params.NZ, _L.PREC[precision], device)
+                         params.NZ, _L.PREC[precision], device, int(getattr(params, "fd_order", 8)))
         h = C.c_void_p()
         rc = self.L.owt_create(C.byref(p), C.byref(h))
         if rc != _L.OK:

@@ -172,6 +172,21 @@ class PortOracle(_Common):
         self.lib.port_time_transforms.restype = C.c_double
         self.lib.port_set_wall_velocity.argtypes = [_dp, _dp]
         self.lib.port_set_wall_velocity.restype = C.c_int
+        self.lib.port_set_fd_order.argtypes = [C.c_int]
+        self.lib.port_set_fd_order.restype = C.c_int
+        self.lib.port_get_stencil.argtypes = [C.c_int, _dp, _dp]
+        self.lib.port_get_stencil.restype = C.c_int
+
+    def set_fd_order(self, order):
+        """Interior compact-FD order (8: the reference's, 6); takes effect at init."""
+        self._chk(self.lib.port_set_fd_order(int(order)), "set_fd_order")
+
+    def stencil(self, which):
+        """The raw A_n, B_n (n = which) on the uniform s-grid, dense [NY, NY]."""
+        a = np.empty(self.NY * self.NY)
+        b = np.empty(self.NY * self.NY)
+        self._chk(self.lib.port_get_stencil(int(which), _ptr(a), _ptr(b)), "get_stencil")
+        return a.reshape(self.NY, self.NY), b.reshape(self.NY, self.NY)
 
     def set_wall_velocity(self, bottom, top):
         """Wall blowing/suction [NZ, NX/2] complex per wall; None, None: no-slip."""

@@ -114,14 +114,22 @@ void matvec(const Dense &m, const cplx *v, cplx *out) {
   }
 }
 
+// Interior order of D1-D3: 8 = the reference's schemes; 6 = the sixth-order
+// tridiagonal schemes (alpha 1/3, 2/11, 7/16) on the interior rows (D2 from
+// row 3 inward), every boundary row as the reference's.  Not in the reference
+// (hard-wired 8th order); the GPU library's fd_order option.
+int g_fd_order = 8;
+
 // Compact finite-difference stencils (src/compdiff.hpp), written into dense
 // matrices on the uniform s-grid with spacing h.
 void stencils(long N, double h, Dense A[4], Dense B[4]) {
+  const bool six = g_fd_order == 6;
   for (int q = 0; q < 4; ++q) { A[q] = Dense(N); B[q] = Dense(N); }
   // 1st derivative: 8th-order interior, 4th-order closures (compdiff.hpp:11-69).
   {
     Dense &a = A[0], &b = B[0];
-    const double al = 4.0 / 9.0, be = 1.0 / 36.0, ca = 40.0 / 27.0, cb = 25.0 / 54.0;
+    const double al = six ? 1.0 / 3.0 : 4.0 / 9.0, be = six ? 0.0 : 1.0 / 36.0;
+    const double ca = six ? 14.0 / 9.0 : 40.0 / 27.0, cb = six ? 1.0 / 9.0 : 25.0 / 54.0;
     for (long i = 2; i < N - 2; ++i) {
       a(i, i - 2) = be; a(i, i - 1) = al; a(i, i) = 1.0; a(i, i + 1) = al; a(i, i + 2) = be;
       b(i, i - 2) = -cb / (4 * h); b(i, i - 1) = -ca / (2 * h); b(i, i + 1) = ca / (2 * h); b(i, i + 2) = cb / (4 * h);
@@ -139,8 +147,12 @@ void stencils(long N, double h, Dense A[4], Dense B[4]) {
   {
     Dense &a = A[1], &b = B[1];
     const double h2 = std::pow(h, 2);
-    const double al = 344.0 / 1179.0, be = 23.0 / 2358.0, ca = 320.0 / 393.0, cb = 310.0 / 393.0;
+    // sixth order on rows 3..N-4 only: rows 1, N-2 are the sixth-order scheme
+    // centred on nodes 2, N-3, so rows 2, N-3 keep the reference's scheme
     for (long i = 2; i < N - 2; ++i) {
+      const bool s6 = six && i >= 3 && i <= N - 4;
+      const double al = s6 ? 2.0 / 11.0 : 344.0 / 1179.0, be = s6 ? 0.0 : 23.0 / 2358.0;
+      const double ca = s6 ? 12.0 / 11.0 : 320.0 / 393.0, cb = s6 ? 3.0 / 11.0 : 310.0 / 393.0;
       a(i, i - 2) = be; a(i, i - 1) = al; a(i, i) = 1.0; a(i, i + 1) = al; a(i, i + 2) = be;
       b(i, i - 2) = cb / (4 * h2); b(i, i - 1) = ca / h2; b(i, i) = -2 * cb / (4 * h2) - 2 * ca / h2;
       b(i, i + 1) = ca / h2; b(i, i + 2) = cb / (4 * h2);
@@ -163,7 +175,8 @@ void stencils(long N, double h, Dense A[4], Dense B[4]) {
   {
     Dense &a = A[2], &b = B[2];
     const double h3 = std::pow(h, 3);
-    const double al = 147.0 / 332.0, be = 1.0 / 166.0, ca = 160.0 / 83.0, cb = -5.0 / 166.0;
+    const double al = six ? 7.0 / 16.0 : 147.0 / 332.0, be = six ? 0.0 : 1.0 / 166.0;
+    const double ca = six ? 2.0 : 160.0 / 83.0, cb = six ? -1.0 / 8.0 : -5.0 / 166.0;
     for (long i = 3; i < N - 3; ++i) {
       a(i, i - 2) = be; a(i, i - 1) = al; a(i, i) = 1.0; a(i, i + 1) = al; a(i, i + 2) = be;
       b(i, i - 3) = -cb / (8 * h3); b(i, i - 2) = -ca / (2 * h3); b(i, i - 1) = ca / h3 + 3 * cb / (8 * h3);
@@ -642,6 +655,20 @@ int guarded(F &&f) {
 
 extern "C" {
 
+int port_set_fd_order(int order) {
+  if (order != 6 && order != 8) return 1;
+  g_fd_order = order;
+  return 0;
+}
+int port_get_stencil(int which, double *a, double *b) {
+  return guarded([&] {
+    if (which < 1 || which > 4) throw std::invalid_argument("stencil index");
+    Dense A[4], B[4];
+    stencils(g_port.NY, g_port.ds, A, B);
+    std::memcpy(a, A[which - 1].a.data(), A[which - 1].a.size() * sizeof(double));
+    std::memcpy(b, B[which - 1].a.data(), B[which - 1].a.size() * sizeof(double));
+  });
+}
 int port_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
   return omp_get_max_threads();

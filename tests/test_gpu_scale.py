@@ -69,3 +69,24 @@ def test_mixed_precision_rhs_error(gpu_lib, big):
         assert errs[n] < 1e-6, n
     for n in ("Hv", "Hg"):
         assert errs[n] < 1e-4, n
+
+
+def test_mixed_precision_profiles_after_500_steps(gpu_lib, big):
+    """Re_tau=550, 384x257x384, dt=0.002: mean-U and RMS profiles after 500
+    steps of the mixed-precision step against the FP64 step from the same
+    seeded state (deviation relative to each profile's maximum)."""
+    from owt.solver import GpuSolver
+    p, (u, v, w) = big
+    stats = {}
+    for prec in ("fp64", "mixed"):
+        s = GpuSolver(p, precision=prec)
+        s.use_graph(True)
+        s.init_fields(u, v, w)
+        s.time_Integration(500)
+        stats[prec] = s.statistics()
+        s.close()
+    dev = {k: float(np.abs(stats["mixed"][k] - stats["fp64"][k]).max() / np.abs(stats["fp64"][k]).max())
+           for k in ("U", "u_rms", "v_rms", "w_rms", "uv")}
+    print("mixed vs fp64 after 500 steps, max deviation / profile max:",
+          {k: f"{x:.2e}" for k, x in dev.items()})
+    assert all(x < 1e-3 for x in dev.values())
