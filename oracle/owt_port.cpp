@@ -254,6 +254,8 @@ struct Port {
 
   void init(double dt_, double dkx_, double dkz_, long nx, long ny, long nz, double al, double nu_) {
     dt = dt_; dkx = dkx_; dkz = dkz_; NX = nx; NY = ny; NZ = nz; alpha = al; nu = nu_;
+    vw_bot.clear();  // a wall velocity belongs to one grid: no-slip after init
+    vw_top.clear();
     if (NY < 7) throw std::invalid_argument("N must be at least 7 for 3rd derivative scheme");
     NXH = NX / 2; NZH = NZ / 2; NX2 = NX / 2 * 3; NZ2 = NZ / 2 * 3;
     // wavenumbers (solver.cpp:25-37), one rank
@@ -570,7 +572,7 @@ struct Port {
         }
         Av(0, 0) = 1.0; Av(N - 1, N - 1) = 1.0; Ag(0, 0) = 1.0; Ag(N - 1, N - 1) = 1.0;
         sv[0] = 0.0; sv[1] = 0.0; sv[N - 2] = 0.0; sv[N - 1] = 0.0;
-        if (!vw_bot.empty()) { sv[0] = vw_bot[m]; sv[N - 1] = vw_top[m]; }
+        if (!vw_bot.empty()) { sv[0] = vw_bot.at(m); sv[N - 1] = vw_top.at(m); }
         sg[0] = 0.0; sg[N - 1] = 0.0;
         lu_factor(Av, pv);
         lu_solve(Av, pv, sv.data());

@@ -98,3 +98,17 @@ def test_torch_autodiff_gradient_matches_port_differences(setup):
         ad = float(np.real(np.vdot(tb.grad.numpy(), db) + np.vdot(tt.grad.numpy(), dt_)))
         assert abs(fd - ad) <= 1e-4 * abs(ad), (q, fd, ad)
     port.set_wall_velocity(None, None)
+
+
+def test_port_init_clears_wall_velocity(setup):
+    """A wall velocity belongs to one grid; re-initialising the port drops it."""
+    from owt.adjoint import seeded_wall_field
+    p, port, vel, _, _ = setup
+    port.set_velocity(*vel)
+    port.step(1)
+    want = port.get("vely")
+    port.set_wall_velocity(seeded_wall_field(p, 1), seeded_wall_field(p, 2))
+    port.init(p.dt, p.dkx, p.dkz, p.NX, p.NY, p.NZ, p.alpha_mesh, p.nu)
+    port.set_velocity(*vel)
+    port.step(1)
+    np.testing.assert_array_equal(port.get("vely"), want)

@@ -51,6 +51,13 @@ def test_blowing_step_matches_oracle(gpu_lib, port_lib):
     port.init(p.dt, p.dkx, p.dkz, p.NX, p.NY, p.NZ, p.alpha_mesh, p.nu)
     port.set_velocity(*seeded_velocity(p, seed=3))
     port.set_wall_velocity(vb, vt)
+    try:
+        _blowing_steps(s, port, vb, vt)
+    finally:
+        port.set_wall_velocity(None, None)
+
+
+def _blowing_steps(s, port, vb, vt):
     for n in range(3):
         s.time_Integration(1)
         port.step(1)
