@@ -196,6 +196,12 @@ int owt_checkpoint_bytes(const owt_handle *h, int64_t *bytes);
 int owt_checkpoint_save(owt_handle *h, void *host, int64_t bytes);
 int owt_checkpoint_load(owt_handle *h, const void *host, int64_t bytes);
 
+/* Keep a copy of the full state in device memory (one slot per handle, about
+ * 15 fields) and return to it later: restart without a host round trip, e.g.
+ * to repeat a run from the same state.  The step counter is restored too. */
+int owt_state_keep(owt_handle *h);
+int owt_state_restore(owt_handle *h);
+
 /* Options and introspection (no counterpart in the reference).
  * OWT_OPT_FORCE_DENSE_BANDS: 1 = sweep the full band of the v-system in every
  *   column instead of skipping structurally-zero interior entries (the two

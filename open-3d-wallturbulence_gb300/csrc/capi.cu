@@ -644,6 +644,8 @@ struct owt_handle {
     int64_t version = -1;  // state_version right after the forward run
   } adj;
   long long staged_step = 0;  // host source of the step-counter upload
+  double2 *kept = nullptr;    // owt_state_keep's image
+  int64_t kept_step = -1;
 
   void free_owned(void *q) {
     for (auto it = owned.begin(); it != owned.end(); ++it)
@@ -1312,6 +1314,24 @@ int owt_get_wall_velocity(owt_handle *h, double *vw_bottom, double *vw_top) {
     ck(cudaMemcpyAsync(vw_bottom, h->vw, b, cudaMemcpyDeviceToHost, h->st), "D2H");
     ck(cudaMemcpyAsync(vw_top, h->vw + h->M, b, cudaMemcpyDeviceToHost, h->st), "D2H");
     ck(cudaStreamSynchronize(h->st), "D2H");
+  });
+}
+
+int owt_state_keep(owt_handle *h) {
+  return guard(h, [&] {
+    if (!h->initialized) throw OwtError(OWT_ERR_STATE, "owt_init_fields (or field uploads) must come first");
+    h->recompute_dirty_q();
+    if (!h->kept) h->kept = dalloc<double2>(h->image_values(), h->owned);
+    h->save_image(h->kept, h->kept_step);
+    ck(cudaStreamSynchronize(h->st), "keep state");
+  });
+}
+
+int owt_state_restore(owt_handle *h) {
+  return guard(h, [&] {
+    if (!h->kept) throw OwtError(OWT_ERR_STATE, "owt_state_keep must come first");
+    ++h->state_version;
+    h->load_image(h->kept, h->kept_step);
   });
 }
 

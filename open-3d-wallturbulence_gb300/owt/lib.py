@@ -83,6 +83,8 @@ def load(path=LIB):
         "owt_checkpoint_save": ([_h, C.c_void_p, C.c_int64], C.c_int),
         "owt_checkpoint_load": ([_h, C.c_void_p, C.c_int64], C.c_int),
         "owt_dy1_noalloc": ([C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "owt_state_keep": ([_h], C.c_int),
+        "owt_state_restore": ([_h], C.c_int),
         "owt_set_wall_velocity": ([_h, _dp, _dp], C.c_int),
         "owt_get_wall_velocity": ([_h, _dp, _dp], C.c_int),
         "owt_drag_forward": ([_h, C.c_int64, C.c_int64, _dp], C.c_int),

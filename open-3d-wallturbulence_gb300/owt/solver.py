@@ -152,6 +152,14 @@ class GpuSolver:
         buf = np.ascontiguousarray(image, dtype=np.uint8)
         self._chk(self.L.owt_checkpoint_load(self.h, buf.ctypes.data_as(C.c_void_p), buf.size))
 
+    def keep_state(self):
+        """Copy the full state to a device-side slot (no host round trip)."""
+        self._chk(self.L.owt_state_keep(self.h))
+
+    def restore_state(self):
+        """Return to the state saved by keep_state."""
+        self._chk(self.L.owt_state_restore(self.h))
+
     def save_checkpoint(self, path):
         self.checkpoint().tofile(path)
 

@@ -120,3 +120,18 @@ def test_batch_step_matches_individual_steps(gpu_lib):
             np.testing.assert_array_equal(a.get(n), c.get(n))
         np.testing.assert_array_equal(a.friction(), c.friction())
     b.close()
+
+
+def test_state_keep_and_restore_on_device(gpu_lib, run):
+    p, s = run
+    s.time_Integration(2)
+    s.keep_state()
+    s.time_Integration(3)
+    first = s.get("vely"), s.get("Hg"), s.friction(), s.step
+    s.restore_state()
+    assert s.step == 2
+    s.time_Integration(3)
+    np.testing.assert_array_equal(s.get("vely"), first[0])
+    np.testing.assert_array_equal(s.get("Hg"), first[1])
+    np.testing.assert_array_equal(s.friction(), first[2])
+    assert s.step == first[3]
