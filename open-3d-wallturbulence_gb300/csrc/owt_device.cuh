@@ -55,82 +55,37 @@ __device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx
   return w;
 }
 
-template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
-template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
-template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-// z + w x and 2 a - b, as fused multiply-adds
-template <typename T> __device__ __forceinline__ cpx<T> cfma(cpx<T> w, cpx<T> x, cpx<T> z) {
-  return mk<T>(fma_t<T>(w.x, x.x, fma_t<T>(-w.y, x.y, z.x)), fma_t<T>(w.x, x.y, fma_t<T>(w.y, x.x, z.y)));
-}
-template <typename T> __device__ __forceinline__ cpx<T> c2m(cpx<T> a, cpx<T> b) {
-  return mk<T>(fma_t<T>((T)2, a.x, -b.x), fma_t<T>((T)2, a.y, -b.y));
-}
-
-// One butterfly of radix R = 4, 2 or 3 (decimation in time, inputs 1.. R-1
-// twiddled), written with fused multiply-adds: x0 + w2 x2 and its partner
-// x0 - w2 x2 = 2 x0 - (x0 + w2 x2) cost 6 FP instructions instead of 8.
-// pin: input x1 is zero (first radix-3 stage over zero padding); pout: output
-// 1 is not needed (last radix-3 stage before truncation).
 template <typename T, bool BACKWARD>
 __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R, int j, int nr, int ns, int base,
-                                          cpx<T> w1, cpx<T> w2, cpx<T> w3, bool twid, bool pin, bool pout) {
+                                          cpx<T> w1, cpx<T> w2, cpx<T> w3, bool twid) {
   if (R == 4) {
-    const cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
-    cpx<T> a, b, c, d;
-    if (twid) {
-      a = cfma<T>(w2, x2, x0);
-      b = c2m<T>(x0, a);
-      const cpx<T> X1 = cmul(x1, w1);
-      c = cfma<T>(w3, x3, X1);
-      d = c2m<T>(X1, c);
-    } else {
-      a = cadd(x0, x2); b = csub(x0, x2); c = cadd(x1, x3); d = csub(x1, x3);
-    }
-    // d * (sign i): forward multiplies by -i, backward by +i
+    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
+    if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); }
+    const cpx<T> t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
+    const cpx<T> d = csub(x1, x3);
+    // t3 = d * (sign i): forward multiplies by -i, backward by +i
     const cpx<T> t3 = BACKWARD ? mk<T>(-d.y, d.x) : mk<T>(d.y, -d.x);
-    dst[base] = cadd(a, c);
-    dst[base + ns] = cadd(b, t3);
-    dst[base + 2 * ns] = csub(a, c);
-    dst[base + 3 * ns] = csub(b, t3);
+    dst[base] = cadd(t0, t2);
+    dst[base + ns] = cadd(t1, t3);
+    dst[base + 2 * ns] = csub(t0, t2);
+    dst[base + 3 * ns] = csub(t1, t3);
   } else if (R == 2) {
-    const cpx<T> x0 = src[j], x1 = src[j + nr];
-    if (twid) {
-      const cpx<T> a = cfma<T>(w1, x1, x0);
-      dst[base] = a;
-      dst[base + ns] = c2m<T>(x0, a);
-    } else {
-      dst[base] = cadd(x0, x1);
-      dst[base + ns] = csub(x0, x1);
-    }
+    cpx<T> x0 = src[j], x1 = src[j + nr];
+    if (twid) x1 = cmul(x1, w1);
+    dst[base] = cadd(x0, x1);
+    dst[base + ns] = csub(x0, x1);
   } else {  // R == 3
+    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
+    if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); }
     const T s60 = (T)0.86602540378443864676372317075294;
-    const cpx<T> x0 = src[j], x2 = src[j + 2 * nr];
-    cpx<T> t, d;
-    if (pin) {  // x1 = 0 (never twiddled: the first stage has none)
-      t = x2;
-      d = mk<T>(-x2.x, -x2.y);
-    } else {
-      const cpx<T> x1 = src[j + nr];
-      if (twid) {
-        const cpx<T> X1 = cmul(x1, w1);
-        t = cfma<T>(w2, x2, X1);
-        d = c2m<T>(X1, t);
-      } else {
-        t = cadd(x1, x2);
-        d = csub(x1, x2);
-      }
-    }
-    const cpx<T> m = mk<T>(fma_t<T>((T)-0.5, t.x, x0.x), fma_t<T>((T)-0.5, t.y, x0.y));
-    // y1 = m + u, y2 = m - u with u = d * (sign i) sin 60
-    const T su = BACKWARD ? -s60 : s60;
+    const cpx<T> t = cadd(x1, x2);
+    const cpx<T> d = csub(x1, x2);
+    const cpx<T> m = mk<T>(x0.x - (T)0.5 * t.x, x0.y - (T)0.5 * t.y);
+    // u = d * (sign i sin60)
+    const cpx<T> u = BACKWARD ? mk<T>(-s60 * d.y, s60 * d.x) : mk<T>(s60 * d.y, -s60 * d.x);
     dst[base] = cadd(x0, t);
-    if (pout) {
-      dst[base + 2 * ns] = mk<T>(fma_t<T>(-su, d.y, m.x), fma_t<T>(su, d.x, m.y));
-    } else {
-      const cpx<T> y1 = mk<T>(fma_t<T>(su, d.y, m.x), fma_t<T>(-su, d.x, m.y));
-      dst[base + ns] = y1;
-      dst[base + 2 * ns] = c2m<T>(m, y1);
-    }
+    dst[base + ns] = cadd(m, u);
+    dst[base + 2 * ns] = csub(m, u);
   }
 }
 
@@ -139,23 +94,14 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
 // and applies it to every (blockDim / (L/R))-th line, so index arithmetic and
 // twiddle loads happen once per stage; a block of L threads keeps every thread
 // busy for radix 2, 3 and 4 when nlines is a multiple of 12.
-//
-// Made for the dealiased (3/2-rule) transforms, L = 3 L/3: the forward
-// transform runs the radices in plan order (radix 3 last) and leaves the
-// middle third of its output [L/3, 2L/3) -- the truncated modes -- unwritten;
-// the backward transform runs them in reverse order (radix 3 first) and
-// assumes the middle third of its input is zero (the padding), which it does
-// not read.  Plans without a factor 3 at the end are run in full.
 template <typename T, bool BACKWARD>
 __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, const FftPlan &p,
                              const cpx<T> *__restrict__ tw) {
   const int L = p.L;
   const int tid = threadIdx.x, nt = blockDim.x;
   int ns = 1;
-  for (int si = 0; si < p.nst; ++si) {
-    const int R = p.R[BACKWARD ? p.nst - 1 - si : si];
-    const bool pin = BACKWARD && si == 0 && R == 3;
-    const bool pout = !BACKWARD && si == p.nst - 1 && R == 3;
+  for (int s = 0; s < p.nst; ++s) {
+    const int R = p.R[s];
     const int nr = L / R;
     const int step = L / (ns * R);
     const int per = nt / nr;  // lines per pass
@@ -172,8 +118,7 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
           if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
         }
         for (int line = lo; line < nlines; line += per)
-          butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, base, w1, w2, w3, twid, pin,
-                                 pout);
+          butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, base, w1, w2, w3, twid);
       }
     } else {
       for (int idx = tid; idx < nlines * nr; idx += nt) {
@@ -187,7 +132,7 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
           if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
         }
         butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, (j - k) * R + k, w1, w2, w3,
-                               twid, pin, pout);
+                               twid);
       }
     }
     __syncthreads();
