@@ -249,23 +249,29 @@ def run_ours(args, rank, world, local_rank):
         del got
 
     # per-stage timing with CUDA events on the library stream (dominant kernel)
-    stage_ms = {}
+    stage_ms, stage_ms_mixed = {}, {}
     if rank == 0:
-        solver.set_precision(args.precision)
         solver.use_graph(False)
-        solver.init_fields(u, v, w)
         st = torch.cuda.ExternalStream(solver.stream)
         reps = max(3, min(10, args.steps))
-        for name, sid in (("modes", 0), ("zback", 4), ("xlamb", 5), ("zfwd", 6), ("nonlinear", 3)):
-            solver.enqueue_stage(sid)
-            solver.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            for _ in range(reps):
+
+        def time_stages(prec, stages, out):
+            solver.set_precision(prec)
+            solver.init_fields(u, v, w)
+            for name, sid in stages:
                 solver.enqueue_stage(sid)
-            e1.record(st)
-            solver.synchronize()
-            stage_ms[name] = e0.elapsed_time(e1) / reps
+                solver.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                for _ in range(reps):
+                    solver.enqueue_stage(sid)
+                e1.record(st)
+                solver.synchronize()
+                out[name] = e0.elapsed_time(e1) / reps
+
+        time_stages("mixed", (("zback", 4), ("xlamb", 5), ("zfwd", 6), ("mean_lamb", 7)), stage_ms_mixed)
+        time_stages(args.precision, (("modes", 0), ("zback", 4), ("xlamb", 5), ("zfwd", 6), ("nonlinear", 3)),
+                    stage_ms)
 
     # end to end through the C ABI with host buffers: every step uploads the
     # full step input (12 history fields, 12 mean vectors, 6 friction values)
@@ -377,6 +383,8 @@ def run_ours(args, rank, world, local_rank):
         line["variants"]["mixed"]["speedup_vs_fp64"] = round(results["fp64"]["ms_per_step"] /
                                                              results["mixed"]["ms_per_step"], 3)
         line["variants"]["mixed"]["rhs_rel_l2_err_vs_fp64"] = {k: float("%.3e" % x) for k, x in rhs_err.items()}
+        if stage_ms_mixed:
+            line["variants"]["mixed"]["transform_stage_ms"] = {k: round(x, 4) for k, x in stage_ms_mixed.items()}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p, args, quick=True)
     if dist is not None:

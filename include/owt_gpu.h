@@ -235,7 +235,9 @@ const char *owt_tuning_report(const owt_handle *h);
  *   2: transforms + products (Lamb vector, three kernels)
  *   3: nonlinear source
  *   4, 5, 6: the three transform kernels alone (z backward, x pass with the
- *            products, z forward) */
+ *            products, z forward)
+ *   7: the FP64 mean-flow terms of the mixed-precision Lamb vector (nothing
+ *      in FP64) */
 #define OWT_STAGE_MODES 0
 #define OWT_STAGE_MEAN 1
 #define OWT_STAGE_LAMB 2
@@ -243,6 +245,7 @@ const char *owt_tuning_report(const owt_handle *h);
 #define OWT_STAGE_ZBACK 4
 #define OWT_STAGE_XLAMB 5
 #define OWT_STAGE_ZFWD 6
+#define OWT_STAGE_MEAN_LAMB 7 /* mixed precision: the FP64 mean-flow terms of the Lamb vector */
 int owt_enqueue_stage(owt_handle *h, int stage);
 
 /* Wall blowing/suction.  The reference imposes v = 0 on both walls through

@@ -386,9 +386,9 @@ struct owt_handle {
     stage_modes();
     launch_advance(d_step, st);
     stage_mean();
-    launch_lamb(xform_args(), precision, st);
+    const int nx = launch_lamb(xform_args(), precision, st);
     launch_nl(nl_args(true), st);
-    launches += 7;
+    launches += 4 + nx;
   }
   void stage_modes() {
     ModeArgs a{};
@@ -528,8 +528,7 @@ struct owt_handle {
     ++launches;
   }
   void lamb_vec(bool explicit_shift) {
-    launch_lamb(xform_args(), precision, st);
-    launches += 3;
+    launches += launch_lamb(xform_args(), precision, st);
     if (explicit_shift) {
       launch_lamb_mean_shift(lxm_ring, lzm_ring, lx, lz, NY, M, d_step, st);
       ++launches;
@@ -1040,6 +1039,7 @@ struct owt_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<cudaEvent_t> events;
+  std::vector<int64_t> step_launches;  // kernels of one captured step, per handle
   ~owt_batch() {
     if (st) cudaStreamSynchronize(st);
     if (exec) cudaGraphExecDestroy(exec);
@@ -1076,7 +1076,10 @@ int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
     for (int q = 0; q < count; ++q) {
       owt_handle *h = b->hs[q];
       ck(cudaStreamWaitEvent(h->st, b->events[0], 0), "fork wait");
+      const int64_t before = h->launches;
       h->enqueue_step();
+      b->step_launches.push_back(h->launches - before);
+      h->launches = before;
       ck(cudaEventRecord(b->events[1 + q], h->st), "join");
       ck(cudaStreamWaitEvent(b->st, b->events[1 + q], 0), "join wait");
     }
@@ -1100,10 +1103,11 @@ int owt_batch_step(owt_batch *b, int64_t nsteps) {
       g_create_error = "batch graph launch failed";
       return OWT_ERR_CUDA;
     }
-    for (owt_handle *h : b->hs) {
+    for (size_t q = 0; q < b->hs.size(); ++q) {
+      owt_handle *h = b->hs[q];
       ++h->steps;
       ++h->state_version;
-      h->launches += 7;
+      h->launches += b->step_launches[q];
     }
   }
   return OWT_OK;
@@ -1274,7 +1278,7 @@ int owt_enqueue_stage(owt_handle *h, int stage) {
       case OWT_STAGE_MEAN: h->stage_mean(); h->launches += 1; break;
       case OWT_STAGE_LAMB: h->launches += launch_lamb(h->xform_args(), h->precision, h->st); break;
       case OWT_STAGE_NONLINEAR: launch_nl(h->nl_args(true), h->st); h->launches += 1; break;
-      case OWT_STAGE_ZBACK: case OWT_STAGE_XLAMB: case OWT_STAGE_ZFWD:
+      case OWT_STAGE_ZBACK: case OWT_STAGE_XLAMB: case OWT_STAGE_ZFWD: case OWT_STAGE_MEAN_LAMB:
         launch_lamb_part(h->xform_args(), h->precision, stage - OWT_STAGE_ZBACK, h->st);
         h->launches += 1;
         break;

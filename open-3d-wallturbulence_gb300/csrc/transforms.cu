@@ -16,10 +16,14 @@
 //  k_zfwd  : per (y, kx tile, field) -- forward FFT of length NZ2, keep slots
 //            k < NZH and NZ + k (k < NZH) -> kz index k + NZH, / NZ2
 //            (FFT.cpp:177-188).  The Nyquist row is kept on this path.
+//  k_mean_lamb (mixed precision only): the FP64 mean-flow terms that the
+//            FP32 transforms leave out, added element-wise.
 //
 // Between kernels the z-padded, x-truncated planes live in HBM as
 // [field][y][z][kx] complex<T>.  T = double (FP64 step) or float (mixed).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "owt_device.cuh"
 #include "solve_kernels.h"
@@ -141,29 +145,6 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   }
 }
 
-// Component f of Ubar x om(k) + u(k) x Obar at mode (kz, kx), in FP64, where
-// Ubar, Obar are the real parts of the (0, 0) modes (the mean flow as the
-// transforms see it) and the fields of the kx = 0 column enter through their
-// Hermitian part, as the real-part extraction of the x transform makes them
-// enter the physical product.  At (0, 0) it is Ubar x Obar.  fld[q] points at
-// row j of field q; Ub, Ob hold the mean vectors of that row.
-__device__ __forceinline__ double2 mean_interaction(const double2 *const *fld, const double *Ub, const double *Ob,
-                                                    int NZ, int NXH, int f, int kz, int kx) {
-  const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
-  if (kz == 0 && kx == 0) return make_double2(Ub[f1] * Ob[f2] - Ub[f2] * Ob[f1], 0.0);
-  auto val = [&](int q) -> double2 {
-    const double2 x = fld[q][(size_t)kz * NXH + kx];
-    if (kx != 0) return x;
-    const int kp = kz == 0 ? 0 : NZ - kz;
-    const double2 y = fld[q][(size_t)kp * NXH];
-    return make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
-  };
-  // (a x b)_f = a_f1 b_f2 - a_f2 b_f1
-  const double2 o1 = val(3 + f1), o2 = val(3 + f2), u1 = val(f1), u2 = val(f2);
-  return make_double2(Ub[f1] * o2.x - Ub[f2] * o1.x + u1.x * Ob[f2] - u2.x * Ob[f1],
-                      Ub[f1] * o2.y - Ub[f2] * o1.y + u1.y * Ob[f2] - u2.y * Ob[f1]);
-}
-
 template <typename T>
 __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
   constexpr int TX = XCfg<T>::TX;
@@ -182,32 +163,77 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
   const cpx<T> *r = fft_lines<T, false>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
   const double sc = a.inv_nz2;
-  const double2 *fld[6];
-  double Ub[3], Ob[3];
-  if (a.mean_split) {
-    const int hd = ring_head(*a.step);
-    const size_t row = (size_t)j * d.NZ * d.NXH;
-    for (int q = 0; q < 6; ++q) {
-      const double2 *base = a.in[q];
-      if (a.ring_mask & (1 << q)) base += (size_t)hd * a.fs;
-      fld[q] = base + row;
-    }
-    for (int q = 0; q < 3; ++q) { Ub[q] = fld[q][0].x; Ob[q] = fld[3 + q][0].x; }
-  }
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
     const int kz = idx / TX, c = idx - kz * TX;
     if (i0 + c < d.NXH) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
       const double2 v = to_d(r[c * ls + slot]);
-      double2 o = make_double2(v.x * sc, v.y * sc);
-      if (a.mean_split && kz != d.NZH) {
-        const double2 l = mean_interaction(fld, Ub, Ob, d.NZ, d.NXH, f, kz, i0 + c);
-        o.x += l.x;
-        o.y += l.y;
-      }
-      dst[(size_t)kz * d.NXH + i0 + c] = o;
+      dst[(size_t)kz * d.NXH + i0 + c] = make_double2(v.x * sc, v.y * sc);
     }
   }
+}
+
+// Mixed precision: add, in FP64, the interaction of the mean flow with the
+// fluctuations that the FP32 transforms left out (mode (0, 0) is zeroed in
+// k_zback): lambda += Ubar x om + u x Obar at every mode and y, Ubar x Obar
+// at (0, 0), nothing on the Nyquist row (it never reaches physical space).
+// Ubar, Obar are the real parts of the (0, 0) modes of row j; the kx = 0
+// column enters through its Hermitian part, as the real-part extraction of
+// the x transform makes it enter the physical product.  One thread per
+// (y, mode), all three components.
+__global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
+  const XformDims d = a.d;
+  const int M = d.NZ * d.NXH;
+  const size_t n = (size_t)d.NY * M;
+  const int hd = ring_head(*a.step);
+  const double2 *base[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    base[q] = a.in[q];
+    if (a.ring_mask & (1 << q)) base[q] += (size_t)hd * a.fs;
+  }
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e / M), m = (int)(e - (size_t)j * M);
+    const int kz = m / d.NXH, kx = m - kz * d.NXH;
+    if (kz == d.NZH) continue;
+    const size_t row = (size_t)j * M;
+    double Ub[3], Ob[3];
+    double2 F[6];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) { Ub[q] = base[q][row].x; Ob[q] = base[3 + q][row].x; }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const double2 x = base[q][row + m];
+      if (kx != 0) {
+        F[q] = x;
+      } else {
+        const double2 y = base[q][row + (size_t)(kz == 0 ? 0 : d.NZ - kz) * d.NXH];
+        F[q] = make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
+      double2 l;
+      if (m == 0) {
+        l = make_double2(Ub[f1] * Ob[f2] - Ub[f2] * Ob[f1], 0.0);
+      } else {
+        // (a x b)_f = a_f1 b_f2 - a_f2 b_f1
+        const double2 o1 = F[3 + f1], o2 = F[3 + f2], u1 = F[f1], u2 = F[f2];
+        l = make_double2(Ub[f1] * o2.x - Ub[f2] * o1.x + u1.x * Ob[f2] - u2.x * Ob[f1],
+                         Ub[f1] * o2.y - Ub[f2] * o1.y + u1.y * Ob[f2] - u2.y * Ob[f1]);
+      }
+      double2 *o = a.out[f] + e;
+      const double2 v = *o;
+      *o = make_double2(v.x + l.x, v.y + l.y);
+    }
+  }
+}
+
+static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
+  const size_t n = (size_t)a.d.NY * a.d.NZ * a.d.NXH;
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_mean_lamb<<<blocks, 256, 0, st>>>(a);
 }
 
 template <typename T>
@@ -226,6 +252,10 @@ static int lamb_t(const XformArgs &a, cudaStream_t st) {
   k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
   dim3 gf((d.NXH + TX - 1) / TX, d.NY, 3);
   k_zfwd<T><<<gf, d.NZ2, sz, st>>>(a);
+  if (a.mean_split) {
+    launch_mean_lamb(a, st);
+    return 4;
+  }
   return 3;
 }
 
@@ -249,8 +279,8 @@ int launch_lamb(const XformArgs &a, int precision, cudaStream_t st) {
   return precision == 0 ? lamb_t<double>(a, st) : lamb_t<float>(a, st);
 }
 
-// One of the three kernels alone (0: z backward, 1: x pass, 2: z forward),
-// for timing.
+// One of the kernels alone (0: z backward, 1: x pass, 2: z forward, 3: the
+// mean-flow term of the mixed-precision Lamb vector), for timing.
 template <typename T>
 static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   const XformDims &d = a.d;
@@ -261,8 +291,10 @@ static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   } else if (part == 1) {
     const size_t nl = (size_t)d.NY * d.NZ2;
     k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
-  } else {
+  } else if (part == 2) {
     k_zfwd<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
+  } else if (a.mean_split) {
+    launch_mean_lamb(a, st);
   }
 }
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st) {
