@@ -82,9 +82,11 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   const size_t line0 = (size_t)blockIdx.x * P;
   const size_t fstride = nlines * d.NXH;
   const cpx<T> *zb = reinterpret_cast<const cpx<T> *>(a.zbuf);
-  // 1. pack field pairs (u,v), (w,ox), (oy,oz) into complex spectra
-  for (int idx = threadIdx.x; idx < 3 * P * d.NX2; idx += blockDim.x) {
-    const int q = idx / d.NX2, mm = idx - q * d.NX2;
+  // 1. pack field pairs (u,v), (w,ox), (oy,oz) into complex spectra; the
+  // block has NX2 threads, thread mm owns point mm of every line
+  const int mm = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < 3 * P; ++q) {
     const int pair = q / P, l = q - pair * P;
     const size_t line = line0 + l;
     cpx<T> z = mk<T>((T)0, (T)0);
@@ -109,8 +111,9 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   cpx<T> *r = fft_lines<T, true>(bufa, bufb, 3 * P, ls, a.px, tw);
   cpx<T> *o = (r == bufa) ? bufb : bufa;
   // 2. lamb = u x omega, packed as (lx + i ly) per line and (lz_l + i lz_l+1)
-  for (int idx = threadIdx.x; idx < P * d.NX2; idx += blockDim.x) {
-    const int l = idx / d.NX2, x = idx - l * d.NX2;
+#pragma unroll
+  for (int l = 0; l < P; ++l) {
+    const int x = mm;
     const cpx<T> uv = r[(0 * P + l) * ls + x], wox = r[(1 * P + l) * ls + x], oyz = r[(2 * P + l) * ls + x];
     const T u = uv.x, v = uv.y, w = wox.x, ox = wox.y, oy = oyz.x, oz = oyz.y;
     const T lx = mul_rn(v, oz) - mul_rn(w, oy);
@@ -126,21 +129,21 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
   cpx<T> *lb = reinterpret_cast<cpx<T> *>(a.lbuf);
   const T half = (T)(0.5 * a.inv_nx2);
   for (int idx = threadIdx.x; idx < P * d.NXH; idx += blockDim.x) {
-    const int l = idx / d.NXH, mm = idx - l * d.NXH;
+    const int l = idx / d.NXH, km = idx - l * d.NXH;
     const size_t line = line0 + l;
     if (line >= nlines) continue;
-    const int mc = (mm == 0) ? 0 : d.NX2 - mm;
+    const int mc = (km == 0) ? 0 : d.NX2 - km;
     {
-      const cpx<T> zm = fo[l * ls + mm], zc = fo[l * ls + mc];
+      const cpx<T> zm = fo[l * ls + km], zc = fo[l * ls + mc];
       // Xa = (Z[m] + conj Z[-m]) / 2 ; Xb = (Z[m] - conj Z[-m]) / (2i)
-      lb[line * d.NXH + mm] = mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
-      lb[fstride + line * d.NXH + mm] = mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half);
+      lb[line * d.NXH + km] = mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
+      lb[fstride + line * d.NXH + km] = mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half);
     }
     {
-      const cpx<T> zm = fo[(P + l / 2) * ls + mm], zc = fo[(P + l / 2) * ls + mc];
+      const cpx<T> zm = fo[(P + l / 2) * ls + km], zc = fo[(P + l / 2) * ls + mc];
       const cpx<T> val = (l & 1) ? mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half)
                                  : mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
-      lb[2 * fstride + line * d.NXH + mm] = val;
+      lb[2 * fstride + line * d.NXH + km] = val;
     }
   }
 }
