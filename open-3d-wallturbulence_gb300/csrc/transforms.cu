@@ -23,8 +23,6 @@
 // [field][y][z][kx] complex<T>.  T = double (FP64 step) or float (mixed).
 #include <cuda_runtime.h>
 
-#include <algorithm>
-
 #include "owt_device.cuh"
 #include "solve_kernels.h"
 
@@ -182,35 +180,35 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
 // at (0, 0), nothing on the Nyquist row (it never reaches physical space).
 // Ubar, Obar are the real parts of the (0, 0) modes of row j; the kx = 0
 // column enters through its Hermitian part, as the real-part extraction of
-// the x transform makes it enter the physical product.  One thread per
-// (y, mode), all three components.
+// the x transform makes it enter the physical product.  Grid: (modes / 256,
+// NY); one thread per mode of row blockIdx.y, all three components.
 __global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
   const XformDims d = a.d;
   const int M = d.NZ * d.NXH;
-  const size_t n = (size_t)d.NY * M;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (m >= M) return;
+  const int kz = m / d.NXH, kx = m - kz * d.NXH;
+  if (kz == d.NZH) return;
   const int hd = ring_head(*a.step);
+  const size_t row = (size_t)j * M, e = row + m;
   const double2 *base[6];
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
-    base[q] = a.in[q];
+    base[q] = a.in[q] + row;
     if (a.ring_mask & (1 << q)) base[q] += (size_t)hd * a.fs;
   }
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const int j = (int)(e / M), m = (int)(e - (size_t)j * M);
-    const int kz = m / d.NXH, kx = m - kz * d.NXH;
-    if (kz == d.NZH) continue;
-    const size_t row = (size_t)j * M;
+  {
     double Ub[3], Ob[3];
     double2 F[6];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) { Ub[q] = base[q][row].x; Ob[q] = base[3 + q][row].x; }
+    for (int q = 0; q < 3; ++q) { Ub[q] = base[q][0].x; Ob[q] = base[3 + q][0].x; }
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const double2 x = base[q][row + m];
+      const double2 x = base[q][m];
       if (kx != 0) {
         F[q] = x;
       } else {
-        const double2 y = base[q][row + (size_t)(kz == 0 ? 0 : d.NZ - kz) * d.NXH];
+        const double2 y = base[q][(kz == 0 ? 0 : d.NZ - kz) * d.NXH];
         F[q] = make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
       }
     }
@@ -234,9 +232,8 @@ __global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
 }
 
 static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
-  const size_t n = (size_t)a.d.NY * a.d.NZ * a.d.NXH;
-  const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
-  k_mean_lamb<<<blocks, 256, 0, st>>>(a);
+  const int M = a.d.NZ * a.d.NXH;
+  k_mean_lamb<<<dim3((M + 255) / 256, a.d.NY), 256, 0, st>>>(a);
 }
 
 template <typename T>
