@@ -240,18 +240,20 @@ struct owt_handle {
     int herr = 0;
     ck(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost), "factor status");
     if (herr) throw OwtError(OWT_ERR_NUMERIC, "LU factorization failed. Matrix A may be singular.");
-    // interior fill inside the compile-time masks? then the sparse solve applies
+    // interior fill of both systems inside the compile-time masks? then the
+    // masked solves apply
     sparse_v = false;
-    if (bv.n % 5 == 0 && bv.n > 2 * 140) {
-      int *d_bad = dalloc<int>(1, owned);
-      ck(cudaMemsetAsync(d_bad, 0, sizeof(int), st), "memset");
-      launch_check_pattern(bv.ab, bv.n, Uq, d_bad, st);
-      ++launches;
-      int nbad = 0;
-      ck(cudaMemcpyAsync(&nbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st), "pattern check");
+    if (bv.n % 5 == 0 && bv.n > 2 * 140 && bg.n % 2 == 0 && bg.n > 2 * 100) {
+      int *d_bad = dalloc<int>(2, owned);
+      ck(cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st), "memset");
+      launch_check_pattern(0, bv.ab, bv.n, Uq, d_bad, st);
+      launch_check_pattern(1, bg.ab, bg.n, Uq, d_bad + 1, st);
+      launches += 2;
+      int nbad[2] = {0, 0};
+      ck(cudaMemcpyAsync(nbad, d_bad, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "pattern check");
       ck(cudaStreamSynchronize(st), "pattern check");
-      sparse_v = (nbad == 0);
-      pattern_violations = nbad;
+      sparse_v = (nbad[0] == 0 && nbad[1] == 0);
+      pattern_violations = nbad[0] + nbad[1];
     }
     rhs_node_v = upload(tv.rhs_node, owned, st);
     rb_col = upload(tg.rb_col, owned, st);

@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
         dg[e] = a.c11[jn] * x;
       }
     };
-    band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
+    if (SPARSE) band_solve_g_sparse(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
+    else band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
   }
   __syncwarp(__activemask());  // the partner's g, DY1 g are read below
 

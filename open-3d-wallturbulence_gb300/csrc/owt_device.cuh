@@ -228,43 +228,54 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 }
 
 // ---------------------------------------------------------------------------
-// The same solve for the v-system, skipping the entries of L and U that are
-// structurally zero in interior columns.  Unknowns are interleaved by node
-// (column c is unknown type c mod 5 of node c / 5); after partial pivoting the
-// nonzero offsets of an interior column depend only on its type.  The masks
-// below are the union over wavenumbers, grid sizes and stretchings observed
-// when the factorization layout was designed; every factorization is checked
-// against them (k_check_pattern) and the dense solve is used if any mode
-// falls outside.  Columns within VB_EDGE of either end are always swept with
-// the full band.  Register rings are padded to multiples of 5 (20, 35) so that
-// the unknown type of every unrolled step is a compile-time constant.
+// The same solve skipping the entries of L and U that are structurally zero in
+// interior columns.  Unknowns are interleaved by node (column c is unknown
+// type c mod NT of node c / NT); after partial pivoting the nonzero offsets of
+// an interior column depend only on its type.  The masks are the union over
+// wavenumbers, grid sizes and stretchings observed when the factorization
+// layout was designed; every factorization is checked against them
+// (k_check_pattern) and the full-band solve is used if any mode falls
+// outside.  Columns within EDGE of either end are always swept with the full
+// band.  Register rings are padded to multiples of NT so that the unknown type
+// of every unrolled step is a compile-time constant (n is a multiple of NT).
+// Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward).
 // ---------------------------------------------------------------------------
 constexpr int VB_EDGE = 60;
-// bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward);
-// argument: unknown type of column c
-// (masks of the equilibrated systems: 31.2 entries per column instead of 51)
-__host__ __device__ constexpr unsigned vmask_l(int ty) {
-  return ty == 0 ? 0x5fffeu : ty == 1 ? 0x6fffeu : ty == 2 ? 0x77ffeu : ty == 3 ? 0x7bffeu : 0x3dffeu;
+constexpr int GB_EDGE = 60;
+// v-system (v, d1..d4 per node): 31.2 entries per column instead of 51
+__host__ __device__ constexpr unsigned long long vmask_l(int ty) {
+  return ty == 0 ? 0x5fffeull : ty == 1 ? 0x6fffeull : ty == 2 ? 0x77ffeull : ty == 3 ? 0x7bffeull : 0x3dffeull;
 }
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
   return ty <= 2 ? 0x1fffeull : ty == 3 ? 0x7ffeull : 0x7feull;
 }
+// omega_y-system (d1, d2 per node): 9 entries per column instead of 18
+__host__ __device__ constexpr unsigned long long gmask_l(int ty) { return ty == 0 ? 0x3eull : 0x1eull; }
+__host__ __device__ constexpr unsigned long long gmask_u(int ty) { return ty == 0 ? 0x1eull : 0x3eull; }
+struct VMasks {
+  __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask_l(ty); }
+  __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask_u(ty); }
+};
+struct GMasks {
+  __host__ __device__ static constexpr unsigned long long l(int ty) { return gmask_l(ty); }
+  __host__ __device__ static constexpr unsigned long long u(int ty) { return gmask_u(ty); }
+};
 
-template <class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
-                                                    int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
-                                                    Out out) {
+template <int KL, int KU, int NT, int W, int WB, int EDGE, class Masks, class Rhs, class YStore, class YLoad,
+          class Out>
+__device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                  int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                  Out out) {
+  static_assert(W >= KL + 1 && W % NT == 0 && WB >= KL + KU + 1 && WB % NT == 0, "ring sizes");
   using V = decltype(rhs(0));
-  constexpr int KL = 18, KU = 15, KV = KL + KU;
-  constexpr int W = 20;    // >= KL + 1, multiple of 5
-  constexpr int WB = 35;   // >= KV + 1, multiple of 5
+  constexpr int KV = KL + KU;
   const size_t sn = (size_t)n * U;
   {
     V w[W];
 #pragma unroll
     for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : vzero<V>();
     for (int j0 = 0; j0 < n; j0 += W) {
-      const bool sparse = (j0 >= VB_EDGE) && (j0 + W - 1 < n - VB_EDGE);
+      const bool sparse = (j0 >= EDGE) && (j0 + W - 1 < n - EDGE);
 #pragma unroll
       for (int s = 0; s < W; ++s) {
         const int j = j0 + s;
@@ -284,7 +295,7 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
           if (sparse) {
 #pragma unroll
             for (int t = 1; t <= KL; ++t)
-              if ((vmask_l(s % 5) >> t) & 1u) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
+              if ((Masks::l(s % NT) >> t) & 1ull) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
           } else {
 #pragma unroll
             for (int t = 1; t <= KL; ++t) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
@@ -299,9 +310,9 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
 #pragma unroll
     for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : vzero<V>();
     for (int jj = 0; jj < n; jj += WB) {
-      // columns n-1-jj .. n-1-jj-(WB-1); n is a multiple of 5, so the type of
-      // column n-1-jj-s is (4 - s) mod 5
-      const bool sparse = (n - 1 - jj < n - VB_EDGE) && (n - 1 - jj - (WB - 1) >= VB_EDGE);
+      // columns n-1-jj .. n-1-jj-(WB-1); the type of column n-1-jj-s is
+      // (NT - 1 - s) mod NT
+      const bool sparse = (n - 1 - jj < n - EDGE) && (n - 1 - jj - (WB - 1) >= EDGE);
 #pragma unroll
       for (int s = 0; s < WB; ++s) {
         const int j = n - 1 - (jj + s);
@@ -312,7 +323,8 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
           if (sparse) {
 #pragma unroll
             for (int t = 1; t <= KV; ++t)
-              if ((vmask_u((4 - s % 5 + 5) % 5) >> t) & 1ull) fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
+              if ((Masks::u((NT - 1 - s % NT + NT) % NT) >> t) & 1ull)
+                fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
           } else {
 #pragma unroll
             for (int t = 1; t <= KV; ++t) fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
@@ -322,6 +334,19 @@ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ a
       }
     }
   }
+}
+
+template <class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                    int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                    Out out) {
+  band_solve_masked<18, 15, 5, 20, 35, VB_EDGE, VMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
+}
+template <class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                    int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                    Out out) {
+  band_solve_masked<6, 6, 2, 8, 14, GB_EDGE, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 
 // ---------------------------------------------------------------------------

@@ -119,28 +119,31 @@ void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sp
   else modes_quad_launch(variant - modes_pair_count(), a, st);
 }
 
-// Every factored v-system must keep its interior fill inside the masks: count
-// the modes whose L or U has a nonzero outside the masks in columns
-// [VB_EDGE, n - VB_EDGE).
+// Every factored system must keep its interior fill inside the masks of its
+// masked solve: count the modes whose L or U has a nonzero outside the masks
+// in columns [EDGE, n - EDGE).
+template <int KL, int KU, int NT, int EDGE, class Masks>
 __global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int *__restrict__ bad) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= U) return;
-  constexpr int KL = 18, KU = 15, KV = KL + KU;
+  constexpr int KV = KL + KU;
   const size_t sn = (size_t)n * U;
   int nbad = 0;
-  for (int c = VB_EDGE; c < n - VB_EDGE; ++c) {
-    const int ty = c % 5;
+  for (int c = EDGE; c < n - EDGE; ++c) {
+    const int ty = c % NT;
     const double *col = ab + (size_t)c * U + u;
     for (int t = 1; t <= KL; ++t)
-      if (!((vmask_l(ty) >> t) & 1u) && col[(size_t)(KV + t) * sn] != 0.0) ++nbad;
+      if (!((Masks::l(ty) >> t) & 1ull) && col[(size_t)(KV + t) * sn] != 0.0) ++nbad;
     for (int t = 1; t <= KV; ++t)
-      if (!((vmask_u(ty) >> t) & 1ull) && col[(size_t)(KV - t) * sn] != 0.0) ++nbad;
+      if (!((Masks::u(ty) >> t) & 1ull) && col[(size_t)(KV - t) * sn] != 0.0) ++nbad;
   }
   if (nbad) atomicAdd(bad, 1);
 }
 
-void launch_check_pattern(const double *ab, int n, int U, int *bad, cudaStream_t st) {
-  k_check_pattern<<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
+// which: 0 the v-system, 1 the omega_y-system
+void launch_check_pattern(int which, const double *ab, int n, int U, int *bad, cudaStream_t st) {
+  if (which == 0) k_check_pattern<18, 15, 5, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
+  else k_check_pattern<6, 6, 2, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
 }
 
 __global__ void k_advance(long long *step) { *step += 1; }
