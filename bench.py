@@ -97,12 +97,12 @@ def stage_work(p, precision="fp64"):
     NY, M, NXH, NZ2, NX2 = p.NY, p.NZ * p.NXH, p.NXH, p.NZ2, p.NX2
     S = 16.0 * NY * M  # bytes per spectral field (complex128)
     P = (16.0 if precision == "fp64" else 8.0) * NY * NZ2 * NXH  # one z-padded plane set
-    # banded systems: v-system 5NY unknowns (kl 18, ku 15), omega_y-system 2NY (6, 6);
+    # banded systems: v-system 4NY+4 unknowns (kl 15, ku 13), omega_y-system 2NY (6, 6);
     # per column and complex rhs: 2 * 2 * (2 kl + ku) flops (forward + backward)
-    fl_modes = M * (5 * NY * 4 * (2 * 18 + 15) + 2 * NY * 4 * (2 * 6 + 6) + 120 * NY)
+    fl_modes = M * ((4 * NY + 4) * 4 * (2 * 15 + 13) + 2 * NY * 4 * (2 * 6 + 6) + 120 * NY)
     fl_fft = lambda n: 5.0 * n * math.log2(n)
     unique = NXH * (p.NZ // 2 + 1)
-    factor_bytes = 8.0 * unique * (5 * NY * (2 * 18 + 15 + 1) + 2 * NY * (2 * 6 + 6 + 1))
+    factor_bytes = 8.0 * unique * ((4 * NY + 4) * (2 * 15 + 13 + 1) + 2 * NY * (2 * 6 + 6 + 1))
     return {
         "modes": {"flops": fl_modes, "bytes": 22 * S + factor_bytes},
         "zback": {"flops": 6 * NXH * NY * fl_fft(NZ2), "bytes": 6 * S + 6 * P},

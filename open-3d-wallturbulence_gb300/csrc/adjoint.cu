@@ -29,6 +29,7 @@
 
 #include "adjoint_kernels.h"
 #include "owt_device.cuh"
+#include "setup_host.h"
 
 namespace owt {
 
@@ -376,11 +377,14 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
     D(a.sgb)[e] = in ? icg * g_ : 0.0;
   }
 
-  // 2. v-system^T: rows with a source node feed Hv, v, DY2 v of the three
-  //    levels; the two wall rows give the wall-velocity gradient
+  // 2. v-system^T: the source adjoint is scattered through the rows' rhs
+  //    tables, then feeds Hv, v, DY2 v of the three levels; the two wall
+  //    rows give the wall-velocity gradient
   {
+    for (int j = 0; j < NY; ++j) D(a.svb)[E(j)] = 0.0;
     auto rhs = [&](int c) -> double {
-      const int jn = c / 5, t = c - 5 * jn;
+      int t, jn;
+      vcol_split(c, NY, t, jn);
       if (t == 0) return D(a.xv0)[E(jn)];
       if (t == 1) return D(a.xv1)[E(jn)];
       if (t == 2) return D(a.xv2)[E(jn)];
@@ -390,24 +394,27 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
     auto yl = [&](int p) -> double { return D(a.yv)[E(p)]; };
     auto out = [&](int p, double z) {
       const double r = z * a.rs_v[(size_t)p * a.U + u];
-      const int j = a.rhs_node_v[p];
-      if (j >= 0) {
-        upd(a.hv, j, r, be0, be1, be2);
-        upd(a.v, j, -k2 * idt * r, al0, al1, al2);
-        upd(a.q, j, idt * r, al0, al1, al2);
-      } else if (j == -2) {
+      const int tag = a.rhs_node_v[p];
+      if (tag == kRhsTable) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double b = a.rbv_val[p * 4 + q];
+          if (b != 0.0) D(a.svb)[E(a.rbv_col[p * 4 + q])] += b * r;
+        }
+      } else if (tag == kRhsWallBottom) {
         D(a.grad)[2 * (size_t)m + comp] += r;
-      } else if (j == -3) {
+      } else if (tag == kRhsWallTop) {
         D(a.grad)[2 * ((size_t)M + m) + comp] += r;
       }
     };
     band_solve_t<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
-    const int edge[4] = {0, 1, NY - 2, NY - 1};  // nodes without a source row
-    for (int q = 0; q < 4; ++q) {
-      const size_t e = E(edge[q]);
-      D(a.hv[0])[e] = 0.0;
-      D(a.v[0])[e] = 0.0;
-      D(a.q[0])[e] = 0.0;
+    // source_v = sum beta Hv_l - k^2/dt sum alpha v_l + sum alpha q_l / dt on
+    // nodes 2..NY-3; the tables reference no other node, so svb is zero there
+    for (int j = 0; j < NY; ++j) {
+      const double r = D(a.svb)[E(j)];
+      upd(a.hv, j, r, be0, be1, be2);
+      upd(a.v, j, -k2 * idt * r, al0, al1, al2);
+      upd(a.q, j, idt * r, al0, al1, al2);
     }
   }
 
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
 
 void launch_adj_modes(const AdjModeArgs &a, cudaStream_t st) {
   const int threads = 2 * a.M;
-  k_adj_modes<18, 15, 6, 6><<<(threads + 127) / 128, 128, 0, st>>>(a);
+  k_adj_modes<15, 13, 6, 6><<<(threads + 127) / 128, 128, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------

@@ -62,12 +62,13 @@ struct AdjModeArgs {
   double inv_dt, nu, inv_h, inv_h2;
   const double *kx, *kz, *c11, *c21, *c22, *inv_cg;
   const double *ab_v; const uint8_t *piv_v; int n_v; const int *rhs_node_v; const double *rs_v;
+  const int *rbv_col; const double *rbv_val;  // v-system rhs tables [n_v][4]
   const double *ab_g; const uint8_t *piv_g; int n_g; const int *rb_col; const double *rb_val; const double *rs_g;
   const double2 *ub, *vb, *wb, *oxb, *gb, *ozb;  // adjoint fields from the Lamb vector
   double2 *v[3], *g[3], *hv[3], *hg[3], *q[3];   // adjoint histories [NY][M]
   double2 *grad;          // [2][M] accumulated d objective / d v_w (bottom, top)
   double2 *yv, *yg;       // scratch [n_v][M], [n_g][M]
-  double2 *xv0, *xv1, *xv2, *xg0, *xg1, *sgb;  // scratch [NY][M]
+  double2 *xv0, *xv1, *xv2, *xg0, *xg1, *sgb, *svb;  // scratch [NY][M]
 };
 
 void launch_adj_nl(const AdjNLArgs &a, cudaStream_t st);

@@ -101,10 +101,11 @@ struct owt_handle {
   int *d_err = nullptr;
   // factors and tables
   BandDev bv, bg, b1, b2;
-  int *rhs_node_v = nullptr, *rb_col = nullptr, *b1_col = nullptr, *b2_col = nullptr;
+  int *rhs_node_v = nullptr, *rb_col = nullptr, *b1_col = nullptr, *b2_col = nullptr, *rbv_col = nullptr;
+  double *rbv_val = nullptr;
   double *rb_val = nullptr, *b1_val = nullptr, *b2_val = nullptr;
   // scratch
-  double2 *sg = nullptr, *dg = nullptr, *yv = nullptr, *yg = nullptr;
+  double2 *sg = nullptr, *dg = nullptr, *yv = nullptr, *yg = nullptr, *sv = nullptr;
   double2 *mean_scratch = nullptr, *mean_dy1 = nullptr;
   double2 *bf = nullptr, *yscr = nullptr, *tmpA = nullptr, *tmpB = nullptr, *tmpC = nullptr, *stage = nullptr;
   void *zbuf = nullptr, *lbuf = nullptr;
@@ -178,7 +179,7 @@ struct owt_handle {
     BandTemplate t1 = build_plain_band(sten, 0);
     BandTemplate t2 = build_plain_band(sten, 1);
     // the kernels are specialised for the bands of the reference's stencils
-    pad_band(tv, 18, 15);
+    pad_band(tv, 15, 13);
     pad_band(tg, 6, 6);
     for (const BandTemplate *t : {&tv, &tg, &t1, &t2})
       if (!band_supported(t->kl, t->ku))
@@ -243,7 +244,7 @@ struct owt_handle {
     // interior fill of both systems inside the compile-time masks? then the
     // masked solves apply
     sparse_v = false;
-    if (bv.n % 5 == 0 && bv.n > 2 * 140 && bg.n % 2 == 0 && bg.n > 2 * 100) {
+    if (bv.n % 4 == 0 && bv.n > 2 * 140 && bg.n % 2 == 0 && bg.n > 2 * 100) {
       int *d_bad = dalloc<int>(2, owned);
       ck(cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st), "memset");
       launch_check_pattern(0, bv.ab, bv.n, Uq, d_bad, st);
@@ -256,6 +257,8 @@ struct owt_handle {
       pattern_violations = nbad[0] + nbad[1];
     }
     rhs_node_v = upload(tv.rhs_node, owned, st);
+    rbv_col = upload(tv.rbv_col, owned, st);
+    rbv_val = upload(tv.rbv_val, owned, st);
     rb_col = upload(tg.rb_col, owned, st);
     rb_val = upload(tg.rb_val, owned, st);
     // B1 / B2 rows as (col, val) x 5
@@ -302,7 +305,7 @@ struct owt_handle {
     hv_ring = dalloc<double2>(3 * fs, owned);
     hg_ring = dalloc<double2>(3 * fs, owned);
     q_ring = dalloc<double2>(3 * fs, owned);
-    for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
+    for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &sv, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
       *f = dalloc<double2>(fs, owned);
     yv = dalloc<double2>((size_t)bv.n * M, owned);
     yg = dalloc<double2>((size_t)bg.n * M, owned);
@@ -404,7 +407,8 @@ struct owt_handle {
     a.rhs_node_v = rhs_node_v; a.rb_col = rb_col; a.rb_val = rb_val; a.inv_cg = inv_cg;
     a.rs_v = bv.rscale; a.rs_g = bg.rscale;
     a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
-    a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg;
+    a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg; a.sv = sv;
+    a.rbv_col = rbv_col; a.rbv_val = rbv_val;
     a.step = d_step;
     a.vw = vw_on ? vw : nullptr;
     launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense,
@@ -633,7 +637,7 @@ struct owt_handle {
     double2 *hist[5][3] = {};  // adjoints of the v, omega_y, Hv, Hg, DY2 v histories
     double2 *mean[4][3] = {};  // U, W, mean lx, mean lz
     double *fric[2][3] = {};   // fx, fz
-    double2 *lb[3] = {}, *fb[6] = {}, *xs[6] = {};
+    double2 *lb[3] = {}, *fb[6] = {}, *xs[7] = {};
     double2 *zbuf = nullptr, *lbuf = nullptr, *yv = nullptr, *yg = nullptr, *mscr = nullptr, *grad = nullptr;
     double *fric_block = nullptr;
     double *obj = nullptr;
@@ -768,6 +772,7 @@ struct owt_handle {
     mo.inv_dt = 1.0 / p.dt; mo.nu = p.nu; mo.inv_h = 1.0 / grid.ds; mo.inv_h2 = 1.0 / (grid.ds * grid.ds);
     mo.kx = kx; mo.kz = kz; mo.c11 = c11; mo.c21 = c21; mo.c22 = c22; mo.inv_cg = inv_cg;
     mo.ab_v = bv.ab; mo.piv_v = bv.piv; mo.n_v = bv.n; mo.rhs_node_v = rhs_node_v; mo.rs_v = bv.rscale;
+    mo.rbv_col = rbv_col; mo.rbv_val = rbv_val;
     mo.ab_g = bg.ab; mo.piv_g = bg.piv; mo.n_g = bg.n; mo.rb_col = rb_col; mo.rb_val = rb_val; mo.rs_g = bg.rscale;
     mo.ub = adj.fb[0]; mo.vb = adj.fb[1]; mo.wb = adj.fb[2]; mo.oxb = adj.fb[3]; mo.gb = adj.fb[4]; mo.ozb = adj.fb[5];
     for (int l = 0; l < 3; ++l) {
@@ -776,7 +781,7 @@ struct owt_handle {
     }
     mo.grad = adj.grad; mo.yv = adj.yv; mo.yg = adj.yg;
     mo.xv0 = adj.xs[0]; mo.xv1 = adj.xs[1]; mo.xv2 = adj.xs[2]; mo.xg0 = adj.xs[3]; mo.xg1 = adj.xs[4];
-    mo.sgb = adj.xs[5];
+    mo.sgb = adj.xs[5]; mo.svb = adj.xs[6];
     launch_adj_modes(mo, st);
     launches += 6;
     check_launch("adjoint step");

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "owt_device.cuh"
+#include "setup_host.h"
 #include "solve_kernels.h"
 
 namespace owt {
@@ -16,7 +17,9 @@ namespace owt {
 //  3. source_v = sum beta Hv_l - k^2/dt sum alpha v_l + DY2(sum alpha v_l)/dt
 //     with DY2 v_l kept as a history of its own (q_l)    (solver.cpp:569-571)
 //  4. v-system: v, D1 v, D2 v                             (solver.cpp:577, 602)
-//     with v = v_w on the walls when blowing/suction is set
+//     with v = v_w on the walls when blowing/suction is set; its rows carry
+//     combinations of source_v (the fourth-derivative rows into which the
+//     interior equations were substituted)
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
 // ---------------------------------------------------------------------------
 template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
@@ -64,6 +67,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
   double *gn = reinterpret_cast<double *>(a.g_ring) + (size_t)hn * fs2 + comp;
   double *qn = reinterpret_cast<double *>(a.q_ring) + (size_t)hn * fs2 + comp;
   double *sg = reinterpret_cast<double *>(a.sg) + comp;
+  double *sv = reinterpret_cast<double *>(a.sv) + comp;
   double *dg = reinterpret_cast<double *>(a.dg) + comp;
   double *yv = reinterpret_cast<double *>(a.yv) + comp;
   double *yg = reinterpret_cast<double *>(a.yg) + comp;
@@ -71,13 +75,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
   const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
   const double idt = a.inv_dt;
 
-  // 1. source_g, walls zero (solver.cpp:573-574, 598-599)
-  for (int j = 0; j < NY; ++j) {
-    const size_t e = E(j);
-    double r = 0.0;
-    if (j != 0 && j != NY - 1)
-      r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
-    sg[e] = r;
+  // 1. source_g, walls zero (solver.cpp:573-574, 598-599), and source_v on
+  //    the nodes with an interior equation (solver.cpp:569-571, 590-596)
+  {
+    const double k2dt = k2 * idt;
+    for (int j = 0; j < NY; ++j) {
+      const size_t e = E(j);
+      double r = 0.0;
+      if (j != 0 && j != NY - 1)
+        r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
+      sg[e] = r;
+      double rv = 0.0;
+      if (j >= 2 && j <= NY - 3) {
+        const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
+        const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
+        rv = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
+      }
+      sv[e] = rv;
+    }
   }
 
   // 2. omega_y-system: g and DY1 g
@@ -112,30 +127,29 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
 
   // 3-5. v-system, then solve_horizontal's components
   {
-    const double k2dt = k2 * idt;
     const bool horiz = !(k2 < 1.e-8);
     const double ik2 = horiz ? 1.0 / k2 : 0.0;
     const double ax = kx * ik2, az = kz * ik2;
     const double kzk2 = kz * k2, kxk2 = kx * k2;
     double d1 = 0.0, d2 = 0.0;
     auto rhs = [&](int p) -> double {
-      const int j = a.rhs_node_v[p];
-      if (j < 0) {
-        // wall rows: v = v_w (blowing/suction) or 0 (solver.cpp:593-596)
-        if (j == -1 || !a.vw) return 0.0;
-        const double *vw = reinterpret_cast<const double *>(a.vw) + (j == -2 ? 0 : 2 * (size_t)M);
-        return vw[2 * m + comp] * a.rs_v[(size_t)p * a.U + u];
+      const int tag = a.rhs_node_v[p];
+      if (tag == kRhsTable) {
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc += a.rbv_val[p * 4 + q] * sv[E(a.rbv_col[p * 4 + q])];
+        return acc * a.rs_v[(size_t)p * a.U + u];
       }
-      const size_t e = E(j);
-      const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
-      const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
-      const double r = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
-      return r * a.rs_v[(size_t)p * a.U + u];
+      // wall rows: v = v_w (blowing/suction) or 0 (solver.cpp:593-596)
+      if (tag == kRhsNone || !a.vw) return 0.0;
+      const double *vw = reinterpret_cast<const double *>(a.vw) + (tag == kRhsWallBottom ? 0 : 2 * (size_t)M);
+      return vw[2 * m + comp] * a.rs_v[(size_t)p * a.U + u];
     };
     auto ys = [&](int p, double y) { yv[E(p)] = y; };
     auto yl = [&](int p) -> double { return yv[E(p)]; };
     auto out = [&](int c, double x) {
-      const int jn = c / 5, t = c - 5 * jn;
+      int t, jn;
+      vcol_split(c, NY, t, jn);
       if (t == 2) {
         d2 = x * a.inv_h2;
       } else if (t == 1) {

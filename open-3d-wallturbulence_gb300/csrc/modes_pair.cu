@@ -10,9 +10,9 @@ struct Variant {
   void (*kernel)(ModeArgs);
 };
 const Variant kVariants[] = {
-    {"pair/128/r166", 128, k_modes<18, 15, 6, 6, true, false, 128, 3>},
-    {"pair/128/r128", 128, k_modes<18, 15, 6, 6, true, false, 128, 4>},
-    {"pair/256/r128", 256, k_modes<18, 15, 6, 6, true, false, 256, 2>},
+    {"pair/128/r166", 128, k_modes<15, 13, 6, 6, true, false, 128, 3>},
+    {"pair/128/r128", 128, k_modes<15, 13, 6, 6, true, false, 128, 4>},
+    {"pair/256/r128", 256, k_modes<15, 13, 6, 6, true, false, 256, 2>},
 };
 }  // namespace
 
@@ -27,7 +27,7 @@ void modes_pair_launch(int v, const ModeArgs &a, cudaStream_t st) {
 // full-band solve (used when a factorization falls outside the sparse masks)
 void modes_dense_launch(const ModeArgs &a, cudaStream_t st) {
   const int bs = 128;
-  k_modes<18, 15, 6, 6, false, false, 128, 3><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
+  k_modes<15, 13, 6, 6, false, false, 128, 3><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
 }
 
 }  // namespace owt

@@ -10,9 +10,9 @@ struct Variant {
   void (*kernel)(ModeArgs);
 };
 const Variant kVariants[] = {
-    {"quad/128/r166", 128, k_modes<18, 15, 6, 6, true, true, 128, 3>},
-    {"quad/128/r128", 128, k_modes<18, 15, 6, 6, true, true, 128, 4>},
-    {"quad/256/r128", 256, k_modes<18, 15, 6, 6, true, true, 256, 2>},
+    {"quad/128/r166", 128, k_modes<15, 13, 6, 6, true, true, 128, 3>},
+    {"quad/128/r128", 128, k_modes<15, 13, 6, 6, true, true, 128, 4>},
+    {"quad/256/r128", 256, k_modes<15, 13, 6, 6, true, true, 256, 2>},
 };
 }  // namespace
 

@@ -229,9 +229,9 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 
 // ---------------------------------------------------------------------------
 // The same solve skipping the entries of L and U that are structurally zero in
-// interior columns.  Unknowns are interleaved by node (column c is unknown
-// type c mod NT of node c / NT); after partial pivoting the nonzero offsets of
-// an interior column depend only on its type.  The masks are the union over
+// interior columns.  Unknowns are interleaved by node, NT per interior node
+// (column c is unknown type (c + OFF) mod NT); after partial pivoting the
+// nonzero offsets of an interior column depend only on its type.  The masks are the union over
 // wavenumbers, grid sizes and stretchings observed when the factorization
 // layout was designed; every factorization is checked against them
 // (k_check_pattern) and the full-band solve is used if any mode falls
@@ -240,14 +240,13 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // of every unrolled step is a compile-time constant (n is a multiple of NT).
 // Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward).
 // ---------------------------------------------------------------------------
-constexpr int VB_EDGE = 60;
+constexpr int VB_EDGE = 48;
 constexpr int GB_EDGE = 60;
-// v-system (v, d1..d4 per node): 31.2 entries per column instead of 51
-__host__ __device__ constexpr unsigned long long vmask_l(int ty) {
-  return ty == 0 ? 0x5fffeull : ty == 1 ? 0x6fffeull : ty == 2 ? 0x77ffeull : ty == 3 ? 0x7bffeull : 0x3dffeull;
-}
+// v-system (v, d1, d2, d3 per interior node): 29.75 entries per column
+// instead of 43
+__host__ __device__ constexpr unsigned long long vmask_l(int) { return 0xfffeull; }
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
-  return ty <= 2 ? 0x1fffeull : ty == 3 ? 0x7ffeull : 0x7feull;
+  return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1fffeull : 0x3ffeull;
 }
 // omega_y-system (d1, d2 per node): 9 entries per column instead of 18
 __host__ __device__ constexpr unsigned long long gmask_l(int ty) { return ty == 0 ? 0x3eull : 0x1eull; }
@@ -261,8 +260,8 @@ struct GMasks {
   __host__ __device__ static constexpr unsigned long long u(int ty) { return gmask_u(ty); }
 };
 
-template <int KL, int KU, int NT, int W, int WB, int EDGE, class Masks, class Rhs, class YStore, class YLoad,
-          class Out>
+template <int KL, int KU, int NT, int OFF, int W, int WB, int EDGE, class Masks, class Rhs, class YStore,
+          class YLoad, class Out>
 __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                   int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                   Out out) {
@@ -295,7 +294,7 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
           if (sparse) {
 #pragma unroll
             for (int t = 1; t <= KL; ++t)
-              if ((Masks::l(s % NT) >> t) & 1ull) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
+              if ((Masks::l((s + OFF) % NT) >> t) & 1ull) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
           } else {
 #pragma unroll
             for (int t = 1; t <= KL; ++t) fms(w[(s + t) % W], col[(size_t)(KV + t) * sn], yj);
@@ -311,7 +310,7 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
     for (int t = 0; t < WB; ++t) w[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : vzero<V>();
     for (int jj = 0; jj < n; jj += WB) {
       // columns n-1-jj .. n-1-jj-(WB-1); the type of column n-1-jj-s is
-      // (NT - 1 - s) mod NT
+      // (OFF - 1 - s) mod NT
       const bool sparse = (n - 1 - jj < n - EDGE) && (n - 1 - jj - (WB - 1) >= EDGE);
 #pragma unroll
       for (int s = 0; s < WB; ++s) {
@@ -323,7 +322,7 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
           if (sparse) {
 #pragma unroll
             for (int t = 1; t <= KV; ++t)
-              if ((Masks::u((NT - 1 - s % NT + NT) % NT) >> t) & 1ull)
+              if ((Masks::u((OFF - 1 - s % NT + 2 * NT) % NT) >> t) & 1ull)
                 fms(w[(s + t) % WB], col[(size_t)(KV - t) * sn], x);
           } else {
 #pragma unroll
@@ -340,13 +339,13 @@ template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<18, 15, 5, 20, 35, VB_EDGE, VMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<15, 13, 4, 2, 16, 32, VB_EDGE, VMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<6, 6, 2, 8, 14, GB_EDGE, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<6, 6, 2, 0, 8, 14, GB_EDGE, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 
 // ---------------------------------------------------------------------------

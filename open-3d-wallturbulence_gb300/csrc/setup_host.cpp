@@ -169,10 +169,15 @@ struct Eq {
   std::map<int, Entry> e;  // by column
   int rhs_node = -1;
   int rb_eq = -1, rb_node = -1;  // omega_y-system: which B_m row feeds the rhs
+  std::vector<std::pair<int, double>> rhs_w;  // v-system: (node, weight) of the rhs
   void add(int col, double t0, double t1 = 0.0, double t2 = 0.0) {
     auto it = e.find(col);
     if (it == e.end()) e[col] = Entry{col, t0, t1, t2};
     else { it->second.t0 += t0; it->second.t1 += t1; it->second.t2 += t2; }
+  }
+  // structural entries only (an exact zero does not widen the column span)
+  void add_nz(int col, double t0, double t1 = 0.0, double t2 = 0.0) {
+    if (t0 != 0.0 || t1 != 0.0 || t2 != 0.0) add(col, t0, t1, t2);
   }
 };
 
@@ -210,6 +215,16 @@ BandTemplate to_band(std::vector<Eq> &eqs, int n, int per_node) {
     }
     bt.rhs_node[p] = q.rhs_node;
   }
+  bt.rbv_col.assign((size_t)n * 4, 0);
+  bt.rbv_val.assign((size_t)n * 4, 0.0);
+  for (int p = 0; p < n; ++p) {
+    const Eq &q = eqs[order[p]];
+    if (q.rhs_w.size() > 4) throw std::logic_error("v-system rhs wider than 4");
+    for (size_t e = 0; e < q.rhs_w.size(); ++e) {
+      bt.rbv_col[(size_t)p * 4 + e] = q.rhs_w[e].first;
+      bt.rbv_val[(size_t)p * 4 + e] = q.rhs_w[e].second;
+    }
+  }
   // keep the equation order for the omega_y rhs tables
   bt.rb_col.assign((size_t)n * 5, 0);
   bt.rb_val.assign((size_t)n * 5, 0.0);
@@ -238,43 +253,69 @@ static void scale_columns(BandTemplate &bt, const std::vector<double> &per_type)
 }
 
 BandTemplate build_v_system(const Grid &g, const Stencils &st, double nu) {
-  const int N = g.N, T = 5;
+  const int N = g.N, n = 4 * N + 4;
+  auto bnd = [&](int j) { return j < 2 || j >= N - 2; };
+  auto V = [&](int t, int j) { return vcol(t, j, N); };
   std::vector<Eq> eqs;
-  eqs.reserve((size_t)T * N);
-  auto V = [&](int c) { return T * c; };
-  auto D = [&](int m, int c) { return T * c + m; };  // m = 1..4
-  for (int j = 0; j < N; ++j) {
+  eqs.reserve(n);
+  // boundary rows (solver.cpp:581-596): v = v_w and DY1 v = 0 on both walls
+  for (int j : {0, 1, N - 2, N - 1}) {
     Eq e;
-    if (j == 0 || j == N - 1) {
-      e.add(V(j), 1.0);
-      e.rhs_node = j == 0 ? kRhsWallBottom : kRhsWallTop;
-    } else if (j == 1) {
-      e.add(D(1, 0), g.c11[0]);
-    } else if (j == N - 2) {
-      e.add(D(1, N - 1), g.c11[N - 1]);
-    } else {
-      // t1 multiplies a = gamma0/dt + 2 nu k^2, t2 multiplies b = nu k^4 + gamma0 k^2/dt
-      e.add(V(j), 0.0, 0.0, -1.0);
-      e.add(D(1, j), -nu * g.c41[j], g.c21[j]);
-      e.add(D(2, j), -nu * g.c42[j], g.c22[j]);
-      e.add(D(3, j), -nu * g.c43[j]);
-      e.add(D(4, j), -nu * g.c44[j]);
-      e.rhs_node = j;
-    }
+    if (j == 0) { e.add(V(0, 0), 1.0); e.rhs_node = kRhsWallBottom; }
+    if (j == 1) e.add(V(1, 0), g.c11[0]);
+    if (j == N - 2) e.add(V(1, N - 1), g.c11[N - 1]);
+    if (j == N - 1) { e.add(V(0, N - 1), 1.0); e.rhs_node = kRhsWallTop; }
     eqs.push_back(e);
   }
-  for (int m = 1; m <= 4; ++m)
+  // A_m d_m - B_m v = 0, m = 1..3
+  for (int m = 1; m <= 3; ++m)
     for (int j = 0; j < N; ++j) {
       Eq e;
       for (int c = 0; c < N; ++c) {
-        if (st.a(m - 1, j, c) != 0.0) e.add(D(m, c), st.a(m - 1, j, c));
-        if (st.b(m - 1, j, c) != 0.0) e.add(V(c), -st.b(m - 1, j, c));
+        if (st.a(m - 1, j, c) != 0.0) e.add(V(m, c), st.a(m - 1, j, c));
+        if (st.b(m - 1, j, c) != 0.0) e.add(V(0, c), -st.b(m - 1, j, c));
       }
       eqs.push_back(e);
     }
-  BandTemplate bt = to_band(eqs, T * N, T);
+  // A_4 d_4 - B_4 v = 0 with d4_c = (r_c + b v_c - G1 d1 - G2 d2 - G3 d3) / G4
+  // on interior nodes c: t1 multiplies a, t2 multiplies b
+  for (int j = 0; j < N; ++j) {
+    Eq e;
+    for (int c = 0; c < N; ++c) {
+      const double a4 = st.a(3, j, c);
+      if (a4 == 0.0) continue;
+      if (bnd(c)) {
+        e.add(V(4, c), a4);
+        continue;
+      }
+      const double w = a4 / (-nu * g.c44[c]);
+      e.add_nz(V(0, c), 0.0, 0.0, w);
+      e.add_nz(V(1, c), w * nu * g.c41[c], -w * g.c21[c]);
+      e.add_nz(V(2, c), w * nu * g.c42[c], -w * g.c22[c]);
+      e.add_nz(V(3, c), w * nu * g.c43[c]);
+      e.rhs_w.push_back({c, -w});
+    }
+    for (int c = 0; c < N; ++c)
+      if (st.b(3, j, c) != 0.0) e.add(V(0, c), -st.b(3, j, c));
+    e.rhs_node = e.rhs_w.empty() ? kRhsNone : kRhsTable;
+    eqs.push_back(e);
+  }
+  if ((int)eqs.size() != n) throw std::logic_error("v-system: equation count");
+  BandTemplate bt = to_band(eqs, n, 4);
+  // column scaling: unknown of type t is solved for as h^t d_t
   const double h = g.ds;
-  scale_columns(bt, {1.0, 1.0 / h, 1.0 / (h * h), 1.0 / (h * h * h), 1.0 / (h * h * h * h)});
+  const int nb = bt.kl + bt.ku + 1;
+  for (int c = 0; c < n; ++c) {
+    int t = 0, j = 0;
+    vcol_split(c, N, t, j);
+    const double f = 1.0 / std::pow(h, t);
+    for (int b = 0; b < nb; ++b) {
+      const size_t at = (size_t)b * n + c;
+      bt.t0[at] *= f;
+      bt.t1[at] *= f;
+      bt.t2[at] *= f;
+    }
+  }
   return bt;
 }
 

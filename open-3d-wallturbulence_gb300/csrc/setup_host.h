@@ -10,11 +10,17 @@
 // built from DYn = sum_m diag(c_nm) A_m^-1 B_m.  The same equations are banded
 // when the compact derivatives d_m = A_m^-1 B_m v are kept as unknowns:
 //
-//   v-system, 5 unknowns per node (v, d1, d2, d3, d4):
-//     A_m d_m - B_m v = 0                                  (m = 1..4, all rows)
-//     (a c21 - nu c41) d1 + (a c22 - nu c42) d2 - nu c43 d3 - nu c44 d4 - b v = r
-//                                  (rows 2..NY-3; a, b as in solver.cpp:577)
+//   v-system, unknowns (v, d1, d2, d3) per node and d4 at nodes 0, 1, N-2,
+//   N-1 only.  With G = (a c21 - nu c41, a c22 - nu c42, -nu c43, -nu c44)
+//   (a, b as in solver.cpp:577) the interior equation of node m (2..N-3)
+//     G1 d1 + G2 d2 + G3 d3 + G4 d4 - b v = r
+//   gives d4_m = (r_m + b v_m - G1 d1_m - G2 d2_m - G3 d3_m) / G4_m, which is
+//   substituted into the fourth-derivative rows, so d4 leaves the interior:
+//     A_m d_m - B_m v = 0                                  (m = 1..3, all rows)
+//     sum_m A4[j,m] d4_m - B_4 v = 0 with d4_m substituted where it can be
+//                            (right-hand side -sum_m A4[j,m] r_m / G4_m)
 //     v_0 = 0, c11_0 d1_0 = 0, c11_N-1 d1_N-1 = 0, v_N-1 = 0   (solver.cpp:581-596)
+//   4N + 4 unknowns instead of 5N, and less fill after pivoting.
 //
 //   omega_y-system, reduced to 2 unknowns per node (d1, d2): with
 //   g_j = (r_j + nu c21_j d1_j + nu c22_j d2_j) / cg on interior nodes and
@@ -34,11 +40,17 @@
 //
 // Equations are ordered by the midpoint of their column span (unknowns
 // interleaved by node); the resulting band widths are structural constants
-// (v-system kl = 18, ku = 15; omega_y-system kl = ku = 6) that the CUDA kernels
+// (v-system kl = 15, ku = 13; omega_y-system kl = ku = 6) that the CUDA kernels
 // take as template parameters.  Band matrices are stored in LAPACK's
 // factorization layout (2kl+ku+1 rows, fill rows first) so that a partial-
 // pivoting band LU (the algorithm of LAPACK dgbtf2/dgbtrs) runs in place.
 #pragma once
+#ifndef __CUDACC__
+#ifndef __host__
+#define __host__
+#define __device__
+#endif
+#endif
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -60,9 +72,28 @@ struct Stencils {
   double b(int n, int i, int j) const { return B[n][(size_t)i * N + j]; }
 };
 
-// rhs_node tags of the two rows v_0 = v_w(bottom), v_N-1 = v_w(top); both are
-// zero (no-slip, src/solver.cpp:593-596) unless wall blowing/suction is set.
-constexpr int kRhsWallBottom = -2, kRhsWallTop = -3;
+// rhs_node tags of the v-system rows: a combination of interior r values
+// (kRhsTable), zero (kRhsNone), and the two rows v_0 = v_w(bottom),
+// v_N-1 = v_w(top), zero (no-slip, src/solver.cpp:593-596) unless wall
+// blowing/suction is set.
+constexpr int kRhsTable = 0, kRhsNone = -1, kRhsWallBottom = -2, kRhsWallTop = -3;
+
+// Column of unknown type t at node j in the v-system (types 0..3 = v, h d1,
+// h^2 d2, h^3 d3 at every node; type 4 = h^4 d4 only at nodes 0, 1, N-2, N-1).
+__host__ __device__ inline int vcol(int t, int j, int N) {
+  return j < 2 ? 5 * j + t : j < N - 2 ? 10 + 4 * (j - 2) + t : 4 * N - 6 + 5 * (j - (N - 2)) + t;
+}
+__host__ __device__ inline void vcol_split(int c, int N, int &t, int &j) {
+  if (c < 10) {
+    j = c / 5; t = c - 5 * j;
+  } else if (c < 4 * N - 6) {
+    const int q = c - 10;
+    j = 2 + (q >> 2); t = q & 3;
+  } else {
+    const int q = c - (4 * N - 6);
+    j = N - 2 + q / 5; t = q - 5 * (q / 5);
+  }
+}
 
 // One equation: coefficients on unknown columns, split as
 // value(k) = t0 + s1(k) * t1 + s2(k) * t2 with per-mode scalars s1, s2.
@@ -78,9 +109,13 @@ struct BandTemplate {
   int per_node = 0;
   // [(kl+ku+1) x n]: entry (i, j) of the ordered matrix at row ku + i - j.
   std::vector<double> t0, t1, t2;
-  // v-system: for each row position, the node whose r feeds it (-1: zero rhs;
-  // kRhsWallBottom / kRhsWallTop: the wall-velocity rows v_0 and v_N-1).
+  // v-system: what feeds the rhs of each row position: kRhsTable (the rbv
+  // table below), kRhsNone (zero), kRhsWallBottom / kRhsWallTop (the
+  // wall-velocity rows v_0 and v_N-1).
   std::vector<int> rhs_node;
+  // v-system: rhs of a kRhsTable row p = sum_e rbv_val[p][e] * r[rbv_col[p][e]]
+  std::vector<int> rbv_col;     // [n x 4]
+  std::vector<double> rbv_val;  // [n x 4]
   // omega_y-system: rhs of row p = (1/cg) sum_e rb_val[p][e] * r[rb_col[p][e]].
   std::vector<int> rb_col;     // [n x 5]
   std::vector<double> rb_val;  // [n x 5]

@@ -94,8 +94,8 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
                         const double *t1, const double *t2, const double *s1, const double *s2, double *rscale,
                         int *info, cudaStream_t st) {
   const int bs = 64, gs = (U + bs - 1) / bs;
-  if (kl == 18 && ku == 15)
-    k_band_factor<18, 15><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
+  if (kl == 15 && ku == 13)
+    k_band_factor<15, 13><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
   else if (kl == 6 && ku == 6)
     k_band_factor<6, 6><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
   else if (kl == 2 && ku == 2)
@@ -103,7 +103,7 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
 }
 
 bool band_supported(int kl, int ku) {
-  return (kl == 18 && ku == 15) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
+  return (kl == 15 && ku == 13) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
 }
 
 // Mode-kernel variants live in modes_pair.cu and modes_quad.cu (separate
@@ -113,7 +113,7 @@ const char *modes_variant_name(int v) {
   return v < modes_pair_count() ? modes_pair_name(v) : modes_quad_name(v - modes_pair_count());
 }
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st) {
-  if (!(klv == 18 && kuv == 15 && klg == 6 && kug == 6)) return;
+  if (!(klv == 15 && kuv == 13 && klg == 6 && kug == 6)) return;
   if (!sparse) { modes_dense_launch(a, st); return; }
   if (variant < modes_pair_count()) modes_pair_launch(variant, a, st);
   else modes_quad_launch(variant - modes_pair_count(), a, st);
@@ -122,7 +122,7 @@ void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sp
 // Every factored system must keep its interior fill inside the masks of its
 // masked solve: count the modes whose L or U has a nonzero outside the masks
 // in columns [EDGE, n - EDGE).
-template <int KL, int KU, int NT, int EDGE, class Masks>
+template <int KL, int KU, int NT, int OFF, int EDGE, class Masks>
 __global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int *__restrict__ bad) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= U) return;
@@ -130,7 +130,7 @@ __global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int
   const size_t sn = (size_t)n * U;
   int nbad = 0;
   for (int c = EDGE; c < n - EDGE; ++c) {
-    const int ty = c % NT;
+    const int ty = (c + OFF) % NT;
     const double *col = ab + (size_t)c * U + u;
     for (int t = 1; t <= KL; ++t)
       if (!((Masks::l(ty) >> t) & 1ull) && col[(size_t)(KV + t) * sn] != 0.0) ++nbad;
@@ -142,8 +142,8 @@ __global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int
 
 // which: 0 the v-system, 1 the omega_y-system
 void launch_check_pattern(int which, const double *ab, int n, int U, int *bad, cudaStream_t st) {
-  if (which == 0) k_check_pattern<18, 15, 5, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
-  else k_check_pattern<6, 6, 2, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
+  if (which == 0) k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
+  else k_check_pattern<6, 6, 2, 0, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
 }
 
 __global__ void k_advance(long long *step) { *step += 1; }

@@ -41,9 +41,10 @@ struct ModeArgs {
   const double *inv_cg;
   const double *rs_v, *rs_g;  // inverse row scales [n][U]
   double inv_h, inv_h2;       // unscaling of solved h d1, h^2 d2
-  double2 *sg, *dg, *yv, *yg;  // scratch
+  double2 *sg, *dg, *yv, *yg, *sv;  // scratch
   const long long *step;
   const double2 *vw;  // wall-normal velocity at the walls [2][M] (bottom, top), or null
+  const int *rbv_col; const double *rbv_val;  // v-system rhs tables [n_v][4]
 };
 
 struct MeanArgs {
