@@ -502,9 +502,82 @@ def cpu_baseline(p, args, quick=False):
                       f"scaled to one full step ({t:.1f} s/step extrapolated)"}
 
 
+def run_adjoint(args, rank, world, local_rank):
+    """Wall-drag gradient at the Re_tau=180 size (128x129x128, dt = 0.005): one
+    evaluation = owt_drag_forward over a 200-step horizon (device images every
+    20 steps) + owt_drag_backward (recompute of each segment + the adjoint
+    steps), timed with CUDA events on the library stream.  Each evaluation is
+    600 steps' work, so the run does one warm-up evaluation and at most 5."""
+    import numpy as np
+    import torch
+    from owt.adjoint import seeded_wall_field
+    from owt.ic import seeded_velocity
+    from owt.params import channel_180
+    from owt.replicas import aggregate, barrier
+    from owt.solver import GpuSolver
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    p = channel_180()
+    horizon, interval = 200, 20
+    s = GpuSolver(p, device=local_rank)
+    s.use_graph(True)
+    s.init_fields(*seeded_velocity(p, seed=0))
+    s.keep_state()
+    s.set_wall_velocity(seeded_wall_field(p, 1), seeded_wall_field(p, 2))
+    st = torch.cuda.ExternalStream(s.stream)
+    k = max(1, min(args.steps, 5))
+
+    def evaluate():
+        s.restore_state()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        J = s.drag_forward(horizon, interval)
+        e1.record(st)
+        g = s.drag_backward()
+        e2.record(st)
+        s.synchronize()
+        return J, g, e0.elapsed_time(e1), e1.elapsed_time(e2)
+
+    evaluate()
+    l0 = s.launch_count
+    barrier()
+    fwd = bwd = 0.0
+    for _ in range(k):
+        J, g, f, b = evaluate()
+        fwd += f
+        bwd += b
+    barrier()
+    launches = s.launch_count - l0
+    ms, rate = aggregate(fwd + bwd, k, device="cuda")
+    dev_bytes = s.info("device_bytes")
+    s.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": "wall-drag gradient evaluations/s, Re_tau=180 128x129x128, 200-step horizon",
+        "value": round(rate, 4), "unit": "gradients/s", "n_gpus": world, "steps": k, "warmup": 1,
+        "ms_per_step": round(ms / k, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic: seeded state (seed 0), seeded wall blowing/suction RMS 1e-3 (seeds 1, 2)",
+        "config": {"workload": "adjoint_channel_180_128x129x128", "horizon_steps": horizon,
+                   "checkpoint_interval": interval, "forward_ms": round(fwd / k, 2),
+                   "backward_ms": round(bwd / k, 2),
+                   "backward_ms_per_step": round(bwd / k / horizon, 3),
+                   "forward_ms_per_step": round(fwd / k / horizon, 3),
+                   "objective": J, "grad_norm": float(np.sqrt(np.vdot(g[0], g[0]).real + np.vdot(g[1], g[1]).real)),
+                   "handle_device_bytes_before_adjoint": dev_bytes,
+                   "warmup_note": "one warm-up evaluation: each is 600 steps of work"},
+        "gpu_launches": launches,
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
+    if args.workload not in ("channel_550", "channel_180"):
+        return {"impl": "reference", "unavailable": f"the reference has no {args.workload} workload: it runs one "
+                                                    "channel per job and has no adjoint"}
     p = workload(args.workload)
     build_port()
     from oracle import PortOracle
@@ -539,7 +612,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--workload", choices=["channel_550", "channel_180", "batch64"], default="channel_550")
+    ap.add_argument("--workload", choices=["channel_550", "channel_180", "batch64", "adjoint"], default="channel_550")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -549,6 +622,8 @@ def main():
         line = run_reference(args, rank, world)
     elif args.workload == "batch64":
         line = run_batch(args, rank, world, local_rank)
+    elif args.workload == "adjoint":
+        line = run_adjoint(args, rank, world, local_rank)
     else:
         line = run_ours(args, rank, world, local_rank)
     if line is not None and rank == 0:
