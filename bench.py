@@ -117,7 +117,7 @@ def stage_work(p, precision="fp64"):
 # a launch at another size by the units the kernel processes (traffic grows in
 # proportion: y-z lines times kx modes for the transforms, modes times NY for the
 # mode kernel).
-NCU_TRAFFIC_128 = {"xlamb_fp64": 200.66e6, "modes": 1.647e9}
+NCU_TRAFFIC_128 = {"xlamb_fp64": 200.66e6, "modes": 1.408e9}
 
 
 def scaled_traffic(kernel, p, precision):
