@@ -212,6 +212,20 @@ __global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
         F[q] = make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
       }
     }
+    // Vbar and Obar_y are the (0, 0) modes of v and omega_y: zero whenever
+    // they start zero (Hv, Hg vanish at k = 0).  Then a row-uniform branch
+    // drops their terms: Ubar x om + u x Obar with Ubar = (U, 0, W), Obar =
+    // (Ox, 0, Oz).
+    if (m != 0 && Ub[1] == 0.0 && Ob[1] == 0.0) {
+      double2 *o0 = a.out[0] + e, *o1 = a.out[1] + e, *o2 = a.out[2] + e;
+      const double2 l0 = *o0, l1 = *o1, l2 = *o2;
+      // x: -W oy + v Oz ; y: W ox - U oz + w Ox - u Oz ; z: U oy - v Ox
+      *o0 = make_double2(l0.x - Ub[2] * F[4].x + F[1].x * Ob[2], l0.y - Ub[2] * F[4].y + F[1].y * Ob[2]);
+      *o1 = make_double2(l1.x + Ub[2] * F[3].x - Ub[0] * F[5].x + F[2].x * Ob[0] - F[0].x * Ob[2],
+                         l1.y + Ub[2] * F[3].y - Ub[0] * F[5].y + F[2].y * Ob[0] - F[0].y * Ob[2]);
+      *o2 = make_double2(l2.x + Ub[0] * F[4].x - F[1].x * Ob[0], l2.y + Ub[0] * F[4].y - F[1].y * Ob[0]);
+      return;
+    }
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
       const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
