@@ -247,8 +247,8 @@ struct owt_handle {
     if (bv.n % 4 == 0 && bv.n > 2 * 140 && bg.n % 2 == 0 && bg.n > 2 * 100) {
       int *d_bad = dalloc<int>(2, owned);
       ck(cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st), "memset");
-      launch_check_pattern(0, bv.ab, bv.n, Uq, d_bad, st);
-      launch_check_pattern(1, bg.ab, bg.n, Uq, d_bad + 1, st);
+      launch_check_pattern(0, bv.ab, bv.piv, bv.n, Uq, d_bad, st);
+      launch_check_pattern(1, bg.ab, bg.piv, bg.n, Uq, d_bad + 1, st);
       launches += 2;
       int nbad[2] = {0, 0};
       ck(cudaMemcpyAsync(nbad, d_bad, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "pattern check");

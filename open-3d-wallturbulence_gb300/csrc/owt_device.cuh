@@ -238,7 +238,8 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // outside.  Columns within EDGE of either end are always swept with the full
 // band.  Register rings are padded to multiples of NT so that the unknown type
 // of every unrolled step is a compile-time constant (n is a multiple of NT).
-// Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward).
+// Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward),
+// row interchange with offset t may occur (pivots).
 // ---------------------------------------------------------------------------
 constexpr int VB_EDGE = 48;
 constexpr int GB_EDGE = 60;
@@ -248,16 +249,23 @@ __host__ __device__ constexpr unsigned long long vmask_l(int) { return 0xfffeull
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
   return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1fffeull : 0x3ffeull;
 }
-// omega_y-system (d1, d2 per node): 9 entries per column instead of 18
+// pivot offsets that occur in interior columns (bit t: offset t; 0 is free)
+__host__ __device__ constexpr unsigned long long vmask_p(int ty) {
+  return ty == 0 ? 0x5eull : ty == 1 ? 0x6eull : ty == 2 ? 0x36ull : 0x3aull;
+}
+// omega_y-system (d1, d2 per node): 9 entries per column instead of 18, and
+// no row interchange in interior columns
 __host__ __device__ constexpr unsigned long long gmask_l(int ty) { return ty == 0 ? 0x3eull : 0x1eull; }
 __host__ __device__ constexpr unsigned long long gmask_u(int ty) { return ty == 0 ? 0x1eull : 0x3eull; }
 struct VMasks {
   __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask_u(ty); }
+  __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask_p(ty); }
 };
 struct GMasks {
   __host__ __device__ static constexpr unsigned long long l(int ty) { return gmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return gmask_u(ty); }
+  __host__ __device__ static constexpr unsigned long long p(int) { return 0ull; }
 };
 
 template <int KL, int KU, int NT, int OFF, int W, int WB, int EDGE, class Masks, class Rhs, class YStore,
@@ -280,9 +288,10 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
         const int j = j0 + s;
         if (j < n) {
           const int off = piv[(size_t)j * U + u];
+          // only the offsets that occur in interior columns are tested there
 #pragma unroll
           for (int t = 1; t <= KL; ++t) {
-            if (off == t) {
+            if ((!sparse || ((Masks::p((s + OFF) % NT) >> t) & 1ull)) && off == t) {
               const V tmp = w[s];
               w[s] = w[(s + t) % W];
               w[(s + t) % W] = tmp;

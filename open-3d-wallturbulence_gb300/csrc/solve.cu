@@ -123,7 +123,8 @@ void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sp
 // masked solve: count the modes whose L or U has a nonzero outside the masks
 // in columns [EDGE, n - EDGE).
 template <int KL, int KU, int NT, int OFF, int EDGE, class Masks>
-__global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int *__restrict__ bad) {
+__global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n, int U,
+                                int *__restrict__ bad) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= U) return;
   constexpr int KV = KL + KU;
@@ -136,14 +137,19 @@ __global__ void k_check_pattern(const double *__restrict__ ab, int n, int U, int
       if (!((Masks::l(ty) >> t) & 1ull) && col[(size_t)(KV + t) * sn] != 0.0) ++nbad;
     for (int t = 1; t <= KV; ++t)
       if (!((Masks::u(ty) >> t) & 1ull) && col[(size_t)(KV - t) * sn] != 0.0) ++nbad;
+    const int off = piv[(size_t)c * U + u];
+    if (off != 0 && !((Masks::p(ty) >> off) & 1ull)) ++nbad;
   }
   if (nbad) atomicAdd(bad, 1);
 }
 
 // which: 0 the v-system, 1 the omega_y-system
-void launch_check_pattern(int which, const double *ab, int n, int U, int *bad, cudaStream_t st) {
-  if (which == 0) k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
-  else k_check_pattern<6, 6, 2, 0, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, n, U, bad);
+void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
+                          cudaStream_t st) {
+  if (which == 0)
+    k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+  else
+    k_check_pattern<6, 6, 2, 0, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
 }
 
 __global__ void k_advance(long long *step) { *step += 1; }

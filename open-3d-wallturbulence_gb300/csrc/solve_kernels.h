@@ -123,7 +123,8 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
 int modes_variant_count();
 const char *modes_variant_name(int v);
-void launch_check_pattern(int which, const double *ab, int n, int U, int *bad, cudaStream_t st);
+void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
+                          cudaStream_t st);
 void launch_advance(long long *step, cudaStream_t st);
 void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st);
 bool mean_prepare(int NY, int n_g);
