@@ -231,9 +231,10 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // The same solve skipping the entries of L and U that are structurally zero in
 // interior columns.  Unknowns are interleaved by node, NT per interior node
 // (column c is unknown type (c + OFF) mod NT); after partial pivoting the
-// nonzero offsets of an interior column depend only on its type.  The masks are the union over
-// wavenumbers, grid sizes and stretchings observed when the factorization
-// layout was designed; every factorization is checked against them
+// nonzero offsets of an interior column depend only on its type.  The masks
+// are the union over wavenumbers, grid sizes, time steps, viscosities and
+// stretchings, found by factorising the band templates on the host over such
+// a sweep; every factorization is checked against them
 // (k_check_pattern) and the full-band solve is used if any mode falls
 // outside.  Columns within EDGE of either end are always swept with the full
 // band.  Register rings are padded to multiples of NT so that the unknown type
@@ -243,9 +244,12 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // ---------------------------------------------------------------------------
 constexpr int VB_EDGE = 48;
 constexpr int GB_EDGE = 60;
-// v-system (v, d1, d2, d3 per interior node): 29.75 entries per column
-// instead of 43
-__host__ __device__ constexpr unsigned long long vmask_l(int) { return 0xfffeull; }
+// v-system (v, d1, d2, d3 per interior node): 26.25 entries per column
+// instead of 43 (the reference's operators; the sixth-order option fills
+// differently and runs the full band)
+__host__ __device__ constexpr unsigned long long vmask_l(int ty) {
+  return ty == 0 ? 0x3ffeull : ty == 1 ? 0x1ffeull : ty == 2 ? 0xffeull : 0x7feull;
+}
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
   return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1fffeull : 0x3ffeull;
 }
