@@ -77,6 +77,8 @@ struct owt_handle {
   int NX = 0, NY = 0, NZ = 0, NXH = 0, NZH = 0, NX2 = 0, NZ2 = 0, M = 0, Uq = 0;
   int precision = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;                    // the mean-mode branch of a step
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<void *> owned;
   int64_t steps = 0;
   int64_t launches = 0;
@@ -129,6 +131,9 @@ struct owt_handle {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     for (void *q : owned) cudaFree(q);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -169,6 +174,9 @@ struct owt_handle {
     for (size_t q = 0; q < rz.size(); ++q) pz.R[q] = rz[q];
     ck(cudaSetDevice(p.device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
 
     // grid, metric, stencils, band templates (host, FP64)
     grid = make_grid(NY, p.alpha_mesh);
@@ -387,10 +395,16 @@ struct owt_handle {
   // One time step.  Every argument is a fixed device pointer; which ring slot
   // is which history level is read from the device step counter, so the same
   // launch sequence (or its CUDA graph) serves every step.
+  // The mean mode runs on a second stream beside the mode kernel (they touch
+  // disjoint data); both read the counter before it advances.
   void enqueue_step() {
+    ck(cudaEventRecord(ev_fork, st), "fork");
+    ck(cudaStreamWaitEvent(st2, ev_fork, 0), "fork wait");
+    stage_mean(true, st2);
+    ck(cudaEventRecord(ev_join, st2), "join");
     stage_modes();
+    ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
     launch_advance(d_step, st);
-    stage_mean();
     const int nx = launch_lamb(xform_args(), precision, st);
     launch_nl(nl_args(true), st);
     launches += 4 + nx;
@@ -414,8 +428,9 @@ struct owt_handle {
     launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense,
                  forced_variant >= 0 ? forced_variant : modes_variant, st);
   }
-  void stage_mean() {
+  void stage_mean(bool pre_advance = false, cudaStream_t s = nullptr) {
     MeanArgs ma{};
+    ma.pre_advance = pre_advance ? 1 : 0;
     ma.NY = NY; ma.M = M; ma.U = Uq; ma.n_g = bg.n;
     ma.inv_dt = 1.0 / p.dt; ma.nu = p.nu; ma.Ly = Ly; ma.inv_cg0 = inv_cg0;
     ma.c11 = c11; ma.c21 = c21; ma.c22 = c22;
@@ -425,7 +440,7 @@ struct owt_handle {
     ma.fx_ring = fx_ring; ma.fz_ring = fz_ring;
     ma.u_field = u; ma.w_field = w; ma.ox_field = ox; ma.oz_field = oz;
     ma.scratch = mean_scratch; ma.dy1 = mean_dy1; ma.step = d_step; ma.err = d_err;
-    launch_mean(ma, mean_smem, st);
+    launch_mean(ma, mean_smem, s ? s : st);
   }
 
   void run_steps(int64_t n) {

@@ -62,6 +62,7 @@ struct MeanArgs {
   double2 *dy1;      // 2*NY
   const long long *step;
   int *err;
+  int pre_advance;   // 1: launched before the step counter advances (concurrently with the mode kernel)
 };
 
 struct NLArgs {
