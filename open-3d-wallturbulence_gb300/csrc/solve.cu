@@ -299,15 +299,13 @@ void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// nonlinear_source (src/solver.cpp:240-260), one thread per real component of
-// a mode (the A1 band LU is real, so the two components are independent):
+// nonlinear_source (src/solver.cpp:240-260), one thread per mode:
 //   Hg = i kz lx - i kx lz,   Hv = -k^2 ly - c11 A1^-1 B1 (i kx lx + i kz lz)
-// written to the level-0 slot; the component threads of mode (0, 0) also
-// record the new mean Lamb vector (src/solver.cpp:296-302).
+// written to the level-0 slot; the thread of mode (0, 0) also records the
+// new mean Lamb vector (src/solver.cpp:296-302).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_nl(NLArgs a) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = tid >> 1, comp = tid & 1;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
   const int k = m / a.NXH, i = m - k * a.NXH;
@@ -315,51 +313,47 @@ __global__ void __launch_bounds__(128) k_nl(NLArgs a) {
   const double k2 = kx * kx + kz * kz;
   const int h = ring_head(*a.step);
   const size_t fs = (size_t)NY * M;
-  auto E = [&](int j) { return 2 * ((size_t)j * M + m) + comp; };
-  const double *lx = reinterpret_cast<const double *>(a.lx), *ly = reinterpret_cast<const double *>(a.ly),
-               *lz = reinterpret_cast<const double *>(a.lz);
-  double *hv = reinterpret_cast<double *>(a.hv_ring + (size_t)h * fs);
-  double *hg = reinterpret_cast<double *>(a.hg_ring + (size_t)h * fs);
-  double *bf = reinterpret_cast<double *>(a.bf), *ys = reinterpret_cast<double *>(a.yscr);
-  // component comp of f = i kx lx + i kz lz and of Hg = i kz lx - i kx lz:
-  // Re(i z) = -Im z, Im(i z) = Re z
-  const int oc = comp ^ 1;
-  const double sgn = comp ? 1.0 : -1.0;
-  auto fval = [&](int j) -> double {
-    const size_t e = 2 * ((size_t)j * M + m) + oc;
-    return sgn * (kx * lx[e] + kz * lz[e]);
+  double2 *hv = a.hv_ring + (size_t)h * fs, *hg = a.hg_ring + (size_t)h * fs;
+  auto fval = [&](int j) -> double2 {
+    const double2 x = a.lx[(size_t)j * M + m], z = a.lz[(size_t)j * M + m];
+    return make_double2(-kx * x.y - kz * z.y, kx * x.x + kz * z.x);
   };
   for (int j = 0; j < NY; ++j) {
-    double acc = 0.0;
+    double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
     for (int e = 0; e < 5; ++e) {
       const double b = a.b1_val[j * 5 + e];
-      if (b != 0.0) acc += b * fval(a.b1_col[j * 5 + e]);
+      if (b != 0.0) {
+        const double2 f = fval(a.b1_col[j * 5 + e]);
+        acc.x += b * f.x;
+        acc.y += b * f.y;
+      }
     }
-    const size_t at = E(j), ao = at - comp + oc;
-    bf[at] = acc;
-    hg[at] = sgn * (kz * lx[ao] - kx * lz[ao]);
+    const size_t at = (size_t)j * M + m;
+    a.bf[at] = acc;
+    const double2 x = a.lx[at], z = a.lz[at];
+    hg[at] = make_double2(-kz * x.y + kx * z.y, kz * x.x - kx * z.x);
   }
-  auto rhs = [&](int p) -> double { return bf[E(p)]; };
-  auto yst = [&](int p, double y) { ys[E(p)] = y; };
-  auto yld = [&](int p) -> double { return ys[E(p)]; };
-  auto out = [&](int c, double d) {
-    const size_t at = E(c);
-    hv[at] = -k2 * ly[at] - a.c11[c] * d;
+  auto rhs = [&](int p) -> double2 { return a.bf[(size_t)p * M + m]; };
+  auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
+  auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
+  auto out = [&](int c, double2 d) {
+    const size_t at = (size_t)c * M + m;
+    const double2 ly = a.ly[at];
+    const double c11 = a.c11[c];
+    hv[at] = make_double2(-k2 * ly.x - c11 * d.x, -k2 * ly.y - c11 * d.y);
   };
-  band_solve<2, 2>(a.ab1, a.piv1, NY, 1, 0, rhs, yst, yld, out);
+  band_solve<2, 2>(a.ab1, a.piv1, NY, 1, 0, rhs, ys, yl, out);
   if (m == 0 && a.lx_mean) {
-    double *lxm = reinterpret_cast<double *>(a.lx_mean + (size_t)h * NY) + comp;
-    double *lzm = reinterpret_cast<double *>(a.lz_mean + (size_t)h * NY) + comp;
     for (int j = 0; j < NY; ++j) {
-      lxm[2 * j] = lx[2 * (size_t)j * M + comp];
-      lzm[2 * j] = lz[2 * (size_t)j * M + comp];
+      a.lx_mean[(size_t)h * NY + j] = a.lx[(size_t)j * M];
+      a.lz_mean[(size_t)h * NY + j] = a.lz[(size_t)j * M];
     }
   }
 }
 
 void launch_nl(const NLArgs &a, cudaStream_t st) {
-  const int bs = 128, gs = (int)((2 * (long long)a.M + bs - 1) / bs);
+  const int bs = 128, gs = (a.M + bs - 1) / bs;
   k_nl<<<gs, bs, 0, st>>>(a);
 }
 
