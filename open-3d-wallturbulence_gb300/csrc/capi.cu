@@ -252,7 +252,8 @@ struct owt_handle {
     // interior fill of both systems inside the compile-time masks? then the
     // masked solves apply
     sparse_v = false;
-    if (bv.n % 4 == 0 && bv.n > 2 * 140 && bg.n % 2 == 0 && bg.n > 2 * 100) {
+    // (systems shorter than the two edges have no masked blocks: full band)
+    if (bv.n % 4 == 0 && bg.n % 2 == 0) {
       int *d_bad = dalloc<int>(2, owned);
       ck(cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st), "memset");
       launch_check_pattern(0, bv.ab, bv.piv, bv.n, Uq, d_bad, st);
