@@ -94,6 +94,7 @@ struct owt_handle {
   size_t fs = 0;  // complex values per spectral field
   // device constants
   double *kx = nullptr, *kz = nullptr, *c11 = nullptr, *c21 = nullptr, *c22 = nullptr, *inv_cg = nullptr;
+  double *nc21 = nullptr, *nc22 = nullptr;  // nu c21, nu c22
   // state
   double2 *v_ring = nullptr, *g_ring = nullptr, *hv_ring = nullptr, *hg_ring = nullptr, *q_ring = nullptr;
   double2 *u = nullptr, *w = nullptr, *ox = nullptr, *oz = nullptr, *lx = nullptr, *ly = nullptr, *lz = nullptr;
@@ -220,6 +221,12 @@ struct owt_handle {
     c11 = upload(grid.c11, owned, st);
     c21 = upload(grid.c21, owned, st);
     c22 = upload(grid.c22, owned, st);
+    {
+      std::vector<double> a21(NY), a22(NY);
+      for (int j = 0; j < NY; ++j) { a21[j] = p.nu * grid.c21[j]; a22[j] = p.nu * grid.c22[j]; }
+      nc21 = upload(a21, owned, st);
+      nc22 = upload(a22, owned, st);
+    }
     inv_cg = upload(icg, owned, st);
     d_step = dalloc<long long>(1, owned);
     d_err = dalloc<int>(1, owned);
@@ -424,6 +431,7 @@ struct owt_handle {
     a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
     a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg; a.sv = sv;
     a.rbv_col = rbv_col; a.rbv_val = rbv_val;
+    a.nc21 = nc21; a.nc22 = nc22;
     a.step = d_step;
     a.vw = vw_on ? vw : nullptr;
     launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, sparse_v && !force_dense,

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
         x *= a.inv_h;
         const size_t e = E(jn);
         double g = 0.0;
-        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nu * a.c21[jn] * x + a.nu * a.c22[jn] * d2) * icg;
+        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nc21[jn] * x + a.nc22[jn] * d2) * icg;
         gn[e] = g;
         dg[e] = a.c11[jn] * x;
       }
@@ -129,7 +129,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
   {
     const bool horiz = !(k2 < 1.e-8);
     const double ik2 = horiz ? 1.0 / k2 : 0.0;
-    const double ax = kx * ik2, az = kz * ik2;
+    const double sgn = comp ? 1.0 : -1.0;
+    const double sax = sgn * kx * ik2, saz = sgn * kz * ik2, sik2 = sgn * ik2;
     const double kzk2 = kz * k2, kxk2 = kx * k2;
     double d1 = 0.0, d2 = 0.0;
     auto rhs = [&](int p) -> double {
@@ -162,26 +163,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
         if (horiz) {
           const double dv = a.c11[jn] * d1;
           const unsigned mask = __activemask();
+          // the partner lane's component of v, DY1 v, DY2 v; of g, DY1 g from memory
           const double xo = __shfl_xor_sync(mask, x, 1), dvo = __shfl_xor_sync(mask, dv, 1),
                        qo = __shfl_xor_sync(mask, q, 1);
-          // full complex values (re, im) of v, DY1 v, DY2 v, g, DY1 g
-          const double vr = comp ? xo : x, vi = comp ? x : xo;
-          const double dvr = comp ? dvo : dv, dvi = comp ? dv : dvo;
-          const double qr = comp ? qo : q, qi = comp ? q : qo;
-          const double *gp = gn - comp, *dgp = dg - comp;
-          const double gr = gp[e], gi = gp[e + 1], dgr = dgp[e], dgi = dgp[e + 1];
+          const double go = gn[e + 1 - 2 * comp], dgo = dg[e + 1 - 2 * comp];
           // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
           // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
-          const double ur = -ax * dvi + az * gi, ui = ax * dvr - az * gr;
-          const double wr = -ax * gi - az * dvi, wi = ax * gr + az * dvr;
-          const double tx = kx * dgr + kz * qr - kzk2 * vr, ty = kx * dgi + kz * qi - kzk2 * vi;
-          const double sx = kz * dgr - kx * qr + kxk2 * vr, sy = kz * dgi - kx * qi + kxk2 * vi;
+          // component c of i z is (2c - 1) times the other component of z
           double *uo = reinterpret_cast<double *>(a.u_out), *wo = reinterpret_cast<double *>(a.w_out);
           double *oxo = reinterpret_cast<double *>(a.ox_out), *ozo = reinterpret_cast<double *>(a.oz_out);
-          uo[e + comp] = comp ? ui : ur;
-          wo[e + comp] = comp ? wi : wr;
-          oxo[e + comp] = comp ? tx * ik2 : -ty * ik2;
-          ozo[e + comp] = comp ? sx * ik2 : -sy * ik2;
+          uo[e + comp] = sax * dvo - saz * go;
+          wo[e + comp] = sax * go + saz * dvo;
+          oxo[e + comp] = (kx * dgo + kz * qo - kzk2 * xo) * sik2;
+          ozo[e + comp] = (kz * dgo - kx * qo + kxk2 * xo) * sik2;
         }
       }
     };

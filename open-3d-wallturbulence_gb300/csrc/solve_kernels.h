@@ -45,6 +45,7 @@ struct ModeArgs {
   const long long *step;
   const double2 *vw;  // wall-normal velocity at the walls [2][M] (bottom, top), or null
   const int *rbv_col; const double *rbv_val;  // v-system rhs tables [n_v][4]
+  const double *nc21, *nc22;                  // nu c21, nu c22
 };
 
 struct MeanArgs {
