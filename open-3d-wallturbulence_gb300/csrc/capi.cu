@@ -528,10 +528,12 @@ struct owt_handle {
   void recompute_dirty_q() {
     for (int sl = 0; sl < 3; ++sl) {
       if (!q_dirty[sl]) continue;
-      double2 *vv = v_ring + (size_t)sl * fs;
-      dapply(1, vv, tmpA);
-      dapply(2, vv, tmpB);
-      launch_combine_y(q_ring + (size_t)sl * fs, tmpA, c21, tmpB, c22, NY, M, st);
+      DY2Args a{};
+      a.NY = NY; a.M = M; a.in = v_ring + (size_t)sl * fs; a.out = q_ring + (size_t)sl * fs;
+      a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
+      a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
+      a.c21 = c21; a.c22 = c22; a.yscr = yscr;
+      launch_dy2(a, st);
       ++launches;
       q_dirty[sl] = false;
     }

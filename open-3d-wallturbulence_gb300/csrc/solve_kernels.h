@@ -87,6 +87,16 @@ struct DApplyArgs {
   double2 *bf, *yscr;
 };
 
+struct DY2Args {
+  int NY, M;
+  const double2 *in;
+  double2 *out;
+  const double *ab1, *ab2; const uint8_t *piv1, *piv2;
+  const int *b1_col, *b2_col; const double *b1_val, *b2_val;
+  const double *c21, *c22;
+  double2 *yscr;
+};
+
 struct VorArgs {
   int NY, NXH, M;
   const double *kx, *kz, *c11;
@@ -132,6 +142,7 @@ void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st);
 bool mean_prepare(int NY, int n_g);
 void launch_nl(const NLArgs &a, cudaStream_t st);
 void launch_dapply(const DApplyArgs &a, cudaStream_t st);
+void launch_dy2(const DY2Args &a, cudaStream_t st);
 void launch_combine_y(double2 *out, const double2 *A, const double *ca, const double2 *B, const double *cb, int NY,
                       int M, cudaStream_t st);
 void launch_vor(const VorArgs &a, cudaStream_t st);
