@@ -524,19 +524,25 @@ struct owt_handle {
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
   }
 
-  // DY2 v for history levels whose v was replaced from the host.
+  // DY2 v for history levels whose v was replaced from the host (one launch).
   void recompute_dirty_q() {
+    DY2Args a{};
+    a.NY = NY; a.M = M;
+    a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
+    a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
+    a.c21 = c21; a.c22 = c22;
+    double2 *scr[3] = {tmpA, tmpB, tmpC};
     for (int sl = 0; sl < 3; ++sl) {
       if (!q_dirty[sl]) continue;
-      DY2Args a{};
-      a.NY = NY; a.M = M; a.in = v_ring + (size_t)sl * fs; a.out = q_ring + (size_t)sl * fs;
-      a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
-      a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
-      a.c21 = c21; a.c22 = c22; a.yscr = yscr;
-      launch_dy2(a, st);
-      ++launches;
+      a.in[a.nf] = v_ring + (size_t)sl * fs;
+      a.out[a.nf] = q_ring + (size_t)sl * fs;
+      a.scr[a.nf] = scr[a.nf];
+      ++a.nf;
       q_dirty[sl] = false;
     }
+    if (!a.nf) return;
+    launch_dy2(a, st);
+    ++launches;
   }
 
   void copy_ring(double2 *ring, size_t n, int from, int to) {

@@ -392,42 +392,42 @@ void launch_dapply(const DApplyArgs &a, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// DY2 f = c21 A1^-1 B1 f + c22 A2^-1 B2 f along y for every mode (the DY2 v
-// history after v levels were replaced), in one pass: two band solves per
-// thread, the B stencils applied inside the right-hand sides.
+// DY2 f = c21 A1^-1 B1 f + c22 A2^-1 B2 f along y for every mode of up to
+// three fields (the DY2 v history after v levels were replaced), in one
+// launch: one thread per field (blockIdx.y), mode and real component (the
+// band systems are real), two band solves per thread with the B stencils
+// applied inside the right-hand sides.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_dy2(DY2Args a) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = tid >> 1, comp = tid & 1, f = blockIdx.y;
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
-  auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
-  auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
-  auto stencil = [&](const int *bc, const double *bv, int p) -> double2 {
-    double2 acc = make_double2(0.0, 0.0);
+  auto E = [&](int j) { return 2 * ((size_t)j * M + m) + comp; };
+  const double *in = reinterpret_cast<const double *>(a.in[f]);
+  double *out = reinterpret_cast<double *>(a.out[f]);
+  double *scr = reinterpret_cast<double *>(a.scr[f]);
+  auto ys = [&](int p, double y) { scr[E(p)] = y; };
+  auto yl = [&](int p) -> double { return scr[E(p)]; };
+  auto stencil = [&](const int *bc, const double *bv, int p) -> double {
+    double acc = 0.0;
 #pragma unroll
     for (int e = 0; e < 5; ++e) {
       const double b = bv[p * 5 + e];
-      if (b != 0.0) {
-        const double2 f = a.in[(size_t)bc[p * 5 + e] * M + m];
-        acc.x += b * f.x;
-        acc.y += b * f.y;
-      }
+      if (b != 0.0) acc += b * in[E(bc[p * 5 + e])];
     }
     return acc;
   };
-  auto rhs1 = [&](int p) -> double2 { return stencil(a.b1_col, a.b1_val, p); };
-  auto out1 = [&](int c, double2 d) { a.out[(size_t)c * M + m] = make_double2(a.c21[c] * d.x, a.c21[c] * d.y); };
+  auto rhs1 = [&](int p) -> double { return stencil(a.b1_col, a.b1_val, p); };
+  auto out1 = [&](int c, double d) { out[E(c)] = a.c21[c] * d; };
   band_solve<2, 2>(a.ab1, a.piv1, NY, 1, 0, rhs1, ys, yl, out1);
-  auto rhs2 = [&](int p) -> double2 { return stencil(a.b2_col, a.b2_val, p); };
-  auto out2 = [&](int c, double2 d) {
-    double2 &q = a.out[(size_t)c * M + m];
-    q = make_double2(q.x + a.c22[c] * d.x, q.y + a.c22[c] * d.y);
-  };
+  auto rhs2 = [&](int p) -> double { return stencil(a.b2_col, a.b2_val, p); };
+  auto out2 = [&](int c, double d) { out[E(c)] += a.c22[c] * d; };
   band_solve<2, 2>(a.ab2, a.piv2, NY, 1, 0, rhs2, ys, yl, out2);
 }
 
 void launch_dy2(const DY2Args &a, cudaStream_t st) {
-  k_dy2<<<(a.M + 127) / 128, 128, 0, st>>>(a);
+  k_dy2<<<dim3((unsigned)((2 * (long long)a.M + 127) / 128), a.nf), 128, 0, st>>>(a);
 }
 
 // Elementwise helpers --------------------------------------------------------

@@ -88,13 +88,12 @@ struct DApplyArgs {
 };
 
 struct DY2Args {
-  int NY, M;
-  const double2 *in;
-  double2 *out;
+  int NY, M, nf;  // nf fields (at most 3)
+  const double2 *in[3];
+  double2 *out[3], *scr[3];  // scr: one field of scratch each
   const double *ab1, *ab2; const uint8_t *piv1, *piv2;
   const int *b1_col, *b2_col; const double *b1_val, *b2_val;
   const double *c21, *c22;
-  double2 *yscr;
 };
 
 struct VorArgs {
