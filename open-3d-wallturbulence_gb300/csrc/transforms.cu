@@ -31,7 +31,7 @@ namespace owt {
 template <typename T> struct XCfg;
 // TX lines per z block, P (y, z) lines per x block (3P FFT lines).  Blocks
 // have as many threads as the line length (NZ2 or NX2, at most 1024).
-template <> struct XCfg<double> { static constexpr int TX = 6; static constexpr int P = 2; };
+template <> struct XCfg<double> { static constexpr int TX = 6; static constexpr int P = 4; };
 template <> struct XCfg<float> { static constexpr int TX = 12; static constexpr int P = 4; };
 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
@@ -68,9 +68,8 @@ __global__ void __launch_bounds__(1024) k_zback(XformArgs a) {
   }
 }
 
-template <typename T>
+template <typename T, int P>
 __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
-  constexpr int P = XCfg<T>::P;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
   const int ls = d.NX2 + 1;
@@ -253,17 +252,33 @@ static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
 template <typename T>
 static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * (d.NZ2 + 1) * sizeof(cpx<T>); }
 template <typename T>
-static size_t smem_x(const XformDims &d) { return 2 * 3 * (size_t)XCfg<T>::P * (d.NX2 + 1) * sizeof(cpx<T>); }
+static size_t smem_x(const XformDims &d, int P) { return 2 * 3 * (size_t)P * (d.NX2 + 1) * sizeof(cpx<T>); }
+// (y, z) lines per x block: XCfg<T>::P where its shared memory fits, else 2
+// (FP64 lines longer than 604 points)
+template <typename T>
+static int x_lines(const XformDims &d) {
+  return smem_x<T>(d, XCfg<T>::P) <= 227 * 1024 ? XCfg<T>::P : 2;
+}
+template <typename T>
+static void launch_x(const XformArgs &a, cudaStream_t st) {
+  const XformDims &d = a.d;
+  const size_t nl = (size_t)d.NY * d.NZ2;
+  if (x_lines<T>(d) == XCfg<T>::P) {
+    constexpr int P = XCfg<T>::P;
+    k_xlamb<T, P><<<(unsigned)((nl + P - 1) / P), d.NX2, smem_x<T>(d, P), st>>>(a);
+  } else {
+    k_xlamb<T, 2><<<(unsigned)((nl + 1) / 2), d.NX2, smem_x<T>(d, 2), st>>>(a);
+  }
+}
 
 template <typename T>
 static int lamb_t(const XformArgs &a, cudaStream_t st) {
   const XformDims &d = a.d;
-  constexpr int TX = XCfg<T>::TX, P = XCfg<T>::P;
-  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  constexpr int TX = XCfg<T>::TX;
+  const size_t sz = smem_z<T>(d);
   dim3 gz((d.NXH + TX - 1) / TX, d.NY, 6);
   k_zback<T><<<gz, d.NZ2, sz, st>>>(a);
-  const size_t nl = (size_t)d.NY * d.NZ2;
-  k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
+  launch_x<T>(a, st);
   dim3 gf((d.NXH + TX - 1) / TX, d.NY, 3);
   k_zfwd<T><<<gf, d.NZ2, sz, st>>>(a);
   if (a.mean_split) {
@@ -275,10 +290,13 @@ static int lamb_t(const XformArgs &a, cudaStream_t st) {
 
 template <typename T>
 static cudaError_t prepare_t(const XformDims &d) {
-  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  const size_t sz = smem_z<T>(d);
   cudaError_t e = raise_smem_limit(k_zback<T>, sz);
   if (e == cudaSuccess) e = raise_smem_limit(k_zfwd<T>, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k_xlamb<T>, sx);
+  if (e == cudaSuccess) {
+    if (x_lines<T>(d) == XCfg<T>::P) e = raise_smem_limit(k_xlamb<T, XCfg<T>::P>, smem_x<T>(d, XCfg<T>::P));
+    else e = raise_smem_limit(k_xlamb<T, 2>, smem_x<T>(d, 2));
+  }
   return e;
 }
 
@@ -298,13 +316,12 @@ int launch_lamb(const XformArgs &a, int precision, cudaStream_t st) {
 template <typename T>
 static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   const XformDims &d = a.d;
-  constexpr int TX = XCfg<T>::TX, P = XCfg<T>::P;
-  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d);
+  constexpr int TX = XCfg<T>::TX;
+  const size_t sz = smem_z<T>(d);
   if (part == 0) {
     k_zback<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), d.NZ2, sz, st>>>(a);
   } else if (part == 1) {
-    const size_t nl = (size_t)d.NY * d.NZ2;
-    k_xlamb<T><<<(unsigned)((nl + P - 1) / P), d.NX2, sx, st>>>(a);
+    launch_x<T>(a, st);
   } else if (part == 2) {
     k_zfwd<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
   } else if (a.mean_split) {

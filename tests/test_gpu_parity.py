@@ -331,3 +331,19 @@ def test_sixth_order_steps_match_oracle(gpu_lib, port_lib, size):
     g8.init_fields(u, v, w)
     g8.time_Integration(nsteps)
     assert rel(g8.get("vely"), g.get("vely")) > 1e-8
+
+
+def test_long_x_lines_step_matches_oracle(gpu_lib, port_lib):
+    """NX = 512 (x lines of 768 points): the FP64 x pass falls back to two
+    (y, z) lines per block, whose shared memory still fits."""
+    from owt.ic import seeded_velocity
+    from owt.params import CaseParams
+    p = CaseParams(dt=0.002, dkx=1.0, dkz=2.0, NX=512, NY=17, NZ=8, alpha_mesh=2.0, nu=1e-3)
+    u, v, w = seeded_velocity(p, seed=7)
+    g, o = gpu_solver(p), port(p)
+    g.init_fields(u, v, w)
+    o.set_velocity(u, v, w)
+    for s in range(2):
+        g.time_Integration(1)
+        o.step(1)
+        compare_state(g, o, 1e-10, tag=f"NX=512 step{s + 1}")
