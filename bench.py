@@ -429,13 +429,13 @@ def run_batch(args, rank, world, local_rank):
             s.synchronize()
     barrier()
     loop_ms, loop_rate = aggregate((time.perf_counter() - t0) * 1e3, 64 * k_loop, device="cuda")
-    # batched: all channels as branches of one graph
+    # batched: one graph launch per step, each kernel over all channels
     b = Batch(solvers)
     b.step(args.warmup)
     b.synchronize()
     st = torch.cuda.ExternalStream(b.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = sum(s.launch_count for s in solvers)
+    l0 = b.launch_count
     with ClockSampler(local_rank) as cs:
         barrier()
         e0.record(st)
@@ -444,11 +444,9 @@ def run_batch(args, rank, world, local_rank):
         b.synchronize()
         barrier()
     ms, rate = aggregate(e0.elapsed_time(e1), 64 * args.steps, device="cuda")
-    launches = sum(s.launch_count for s in solvers) - l0
-    variants = {}
-    for s in solvers:
-        v = s.tuning_report().split("-> ")[-1]
-        variants[v] = variants.get(v, 0) + 1
+    launches = b.launch_count - l0
+    step_launches = b.step_launches
+    tuning = b.tuning_report()
     b.close()
     for s in solvers:
         s.close()
@@ -461,7 +459,8 @@ def run_batch(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic: 64 seeded minimal channels, laminar + seeded perturbation each",
         "config": {"workload": "batch64_minimal_channels", "precision": "mixed", "channels": 64,
-                   "physical_points_total": points, "mode_kernel_variants": variants,
+                   "physical_points_total": points, "kernels_per_batch_step": step_launches,
+                   "mode_kernel_autotune": tuning,
                    "l2": "no flush; per-step state of all channels ~%.1f GB" % (
                        sum(22 * 16 * p.NY * p.NZ * p.NXH for p in ps) / 1e9)},
         "variants": {"serial_loop": {"channel_steps_per_s": round(loop_rate, 3),

@@ -165,17 +165,26 @@ int owt_get_grid(const owt_handle *h, double *y);
 int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
 
 /* Batches of independent channels (no counterpart in the reference, which runs
- * one channel per MPI job).  A batch captures one time step of every handle
- * as parallel branches of a single CUDA graph, so a step of all channels is
- * one graph launch and small channels run concurrently on the GPU.  Handles
- * keep their own state, sizes and parameters (uneven sizes are fine) and
- * must outlive the batch; all must be on one device and initialised.  While
- * a handle is in a batch, step it through the batch only. */
+ * one channel per MPI job).  A batch step is one CUDA graph launch in which
+ * every kernel of the time step runs once over all channels (one launch per
+ * group of up to 64 channels sharing the kernel's block shape); the mode
+ * kernel, which holds every per-mode banded solve of every channel, is a
+ * persistent launch whose resident blocks take work items from a counter.
+ * owt_batch_create times every mode-kernel variant on the batch (the handles'
+ * state is put back afterwards) and keeps the fastest; the report lists the
+ * timings.  Handles keep their own state, sizes and parameters (uneven sizes
+ * are fine) and must outlive the batch; all must be on one device and
+ * initialised, each at most once.  While a handle is in a batch, step it
+ * through the batch only; results are bitwise those of stepping it alone.
+ * Launch counts: all kernels launched by the batch, and those of one step. */
 typedef struct owt_batch owt_batch;
 int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out);
 int owt_batch_step(owt_batch *b, int64_t nsteps);
 int owt_batch_synchronize(owt_batch *b);
 int owt_batch_get_stream(const owt_batch *b, void **stream);
+int owt_batch_get_launch_count(const owt_batch *b, int64_t *count);
+int owt_batch_get_step_launches(const owt_batch *b, int64_t *count);
+const char *owt_batch_tuning_report(const owt_batch *b);
 int owt_batch_destroy(owt_batch *b);
 
 /* Wall-normal statistics of the current velocity (no counterpart in the

@@ -22,13 +22,12 @@ namespace owt {
 //     interior equations were substituted)
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
 // ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD>
+__device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
   // One thread per real component of a mode (the band systems are real).
   // Pair mapping: lanes 2m, 2m+1 are Re, Im of mode m.  Quad mapping: lanes
   // 4u..4u+3 are (Re, Im) of the two modes +kz, -kz of unique mode u, which
   // share one factorization, so four adjacent lanes read the same factors.
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   int m, comp, k, i, kabs;
   if (QUAD) {
     const int uq = tid >> 2, r = tid & 3, sgn = r >> 1;
@@ -184,6 +183,41 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_modes(ModeArgs a) {
   }
 }
 
+// One channel: thread tid of the grid is thread tid of the mapping.
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_modes(const __grid_constant__ ModeArgs a) {
+  mode_body<KLV, KUV, KLG, KUG, SPARSE, QUAD>(a, blockIdx.x * BLOCK + threadIdx.x);
+}
+
+// Every channel of a batch in one persistent launch.  Work items are the
+// BLOCK-thread slices of each channel's mapping, numbered channel by channel
+// in the table's order (the host lists the channels with the longest systems
+// first); resident blocks take items from an atomic counter until none are
+// left, so channels of uneven sizes share the SMs without a tail per channel.
+// The last block to finish resets the counter for the next launch.
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+    k_modes_batch(const __grid_constant__ BatchTable<ModeArgs> t, int *work) {
+  __shared__ int item;
+  const int total = t.start[t.n];
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(work, 1);
+    __syncthreads();
+    const int it = item;
+    __syncthreads();  // every thread has read item before it is overwritten
+    if (it >= total) break;
+    const int c = batch_channel(t.start, t.n, it);
+    mode_body<KLV, KUV, KLG, KUG, SPARSE, QUAD>(t.a[c], (it - t.start[c]) * BLOCK + threadIdx.x);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(work + 1, 1) == (int)gridDim.x - 1) {
+      work[0] = 0;
+      work[1] = 0;
+    }
+  }
+}
+
 
 int modes_pair_count();
 const char *modes_pair_name(int v);
@@ -192,5 +226,13 @@ void modes_dense_launch(const ModeArgs &a, cudaStream_t st);
 int modes_quad_count();
 const char *modes_quad_name(int v);
 void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st);
+
+// Batched launches: the work-item geometry of a variant and the persistent launch.
+ModeBatchShape modes_pair_batch_shape(int v);
+ModeBatchShape modes_quad_batch_shape(int v);
+ModeBatchShape modes_dense_batch_shape();
+void modes_pair_batch_launch(int v, const BatchTable<ModeArgs> &t, int *work, int grid, cudaStream_t st);
+void modes_quad_batch_launch(int v, const BatchTable<ModeArgs> &t, int *work, int grid, cudaStream_t st);
+void modes_dense_batch_launch(const BatchTable<ModeArgs> &t, int *work, int grid, cudaStream_t st);
 
 }  // namespace owt

@@ -119,6 +119,18 @@ void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sp
   else modes_quad_launch(variant - modes_pair_count(), a, st);
 }
 
+// Batched mode kernel: variant -1 is the full-band solve.
+ModeBatchShape modes_batch_shape(int variant) {
+  if (variant < 0) return modes_dense_batch_shape();
+  if (variant < modes_pair_count()) return modes_pair_batch_shape(variant);
+  return modes_quad_batch_shape(variant - modes_pair_count());
+}
+void launch_modes_batch(const BatchTable<ModeArgs> &t, int variant, int *work, int grid, cudaStream_t st) {
+  if (variant < 0) modes_dense_batch_launch(t, work, grid, st);
+  else if (variant < modes_pair_count()) modes_pair_batch_launch(variant, t, work, grid, st);
+  else modes_quad_batch_launch(variant - modes_pair_count(), t, work, grid, st);
+}
+
 // Every factored system must keep its interior fill inside the masks of its
 // masked solve: count the modes whose L or U has a nonzero outside the masks
 // in columns [EDGE, n - EDGE).
@@ -154,6 +166,10 @@ void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n
 
 __global__ void k_advance(long long *step) { *step += 1; }
 void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>>>(step); }
+__global__ void k_advance_batch(const __grid_constant__ StepCounters c) {
+  if ((int)threadIdx.x < c.n) *c.p[threadIdx.x] += 1;
+}
+void launch_advance_batch(const StepCounters &c, cudaStream_t st) { k_advance_batch<<<1, kBatchChannels, 0, st>>>(c); }
 
 // ---------------------------------------------------------------------------
 // Mean mode (solve_mean + solve_friction_force, src/solver.cpp:306-327,
@@ -165,7 +181,7 @@ void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>
 // (the same matrix as solve_mean's A).
 // ---------------------------------------------------------------------------
 template <bool SMEM>
-__global__ void k_mean(MeanArgs a) {
+__device__ __forceinline__ void mean_body(const MeanArgs &a) {
   const int t = threadIdx.x;
   const int NY = a.NY, n = a.n_g;
   const int h = ring_head(*a.step + (a.pre_advance ? 1 : 0));
@@ -280,6 +296,13 @@ __global__ void k_mean(MeanArgs a) {
   }
 }
 
+template <bool SMEM>
+__global__ void k_mean(const __grid_constant__ MeanArgs a) { mean_body<SMEM>(a); }
+
+// every channel of a batch: block c runs channel c's mean mode
+template <bool SMEM>
+__global__ void k_mean_batch(const __grid_constant__ BatchTable<MeanArgs> t) { mean_body<SMEM>(t.a[blockIdx.x]); }
+
 size_t mean_smem_bytes(int NY, int n_g) {
   return (2 * (size_t)NY + 2 * (size_t)n_g) * sizeof(double2) + 19 * (size_t)n_g * sizeof(double) +
          (size_t)n_g * sizeof(double) + 5 * (size_t)n_g * (sizeof(double) + sizeof(int)) +
@@ -298,14 +321,20 @@ void launch_mean(const MeanArgs &a, bool smem, cudaStream_t st) {
   else k_mean<false><<<1, 128, 0, st>>>(a);
 }
 
+// shared memory of the batched launch: the largest channel's
+cudaError_t mean_batch_prepare(size_t smem_bytes) { return raise_smem_limit(k_mean_batch<true>, smem_bytes); }
+void launch_mean_batch(const BatchTable<MeanArgs> &t, bool smem, size_t smem_bytes, cudaStream_t st) {
+  if (smem) k_mean_batch<true><<<t.n, 256, smem_bytes, st>>>(t);
+  else k_mean_batch<false><<<t.n, 128, 0, st>>>(t);
+}
+
 // ---------------------------------------------------------------------------
 // nonlinear_source (src/solver.cpp:240-260), one thread per mode:
 //   Hg = i kz lx - i kx lz,   Hv = -k^2 ly - c11 A1^-1 B1 (i kx lx + i kz lz)
 // written to the level-0 slot; the thread of mode (0, 0) also records the
 // new mean Lamb vector (src/solver.cpp:296-302).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_nl(NLArgs a) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void nl_body(const NLArgs &a, const int m) {
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
   const int k = m / a.NXH, i = m - k * a.NXH;
@@ -352,10 +381,20 @@ __global__ void __launch_bounds__(128) k_nl(NLArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(128) k_nl(const __grid_constant__ NLArgs a) {
+  nl_body(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(128) k_nl_batch(const __grid_constant__ BatchTable<NLArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  nl_body(t.a[c], (blockIdx.x - t.start[c]) * 128 + threadIdx.x);
+}
+
 void launch_nl(const NLArgs &a, cudaStream_t st) {
   const int bs = 128, gs = (a.M + bs - 1) / bs;
   k_nl<<<gs, bs, 0, st>>>(a);
 }
+int nl_batch_blocks(const NLArgs &a) { return (a.M + 127) / 128; }
+void launch_nl_batch(const BatchTable<NLArgs> &t, cudaStream_t st) { k_nl_batch<<<t.start[t.n], 128, 0, st>>>(t); }
 
 // ---------------------------------------------------------------------------
 // d = A_n^-1 B_n f along y for every mode (raw compact derivative on the

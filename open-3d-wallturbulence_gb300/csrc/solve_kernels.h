@@ -6,6 +6,7 @@
 
 #include <mutex>
 
+#include "batch.cuh"
 #include "owt_device.cuh"
 
 namespace owt {
@@ -160,5 +161,35 @@ cudaError_t lamb_prepare(const XformDims &d);
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st);
 size_t lamb_zbuf_bytes(const XformDims &d, int precision);
 size_t lamb_lbuf_bytes(const XformDims &d, int precision);
+
+// Batch tables travel as kernel parameters, which are limited to 32764 bytes.
+static_assert(sizeof(BatchTable<ModeArgs>) <= 32764, "mode-kernel batch table exceeds the kernel parameter limit");
+static_assert(sizeof(BatchTable<XformArgs>) <= 32764, "transform batch table exceeds the kernel parameter limit");
+static_assert(sizeof(BatchTable<MeanArgs>) <= 32764, "mean-mode batch table exceeds the kernel parameter limit");
+static_assert(sizeof(BatchTable<NLArgs>) <= 32764, "nonlinear batch table exceeds the kernel parameter limit");
+
+// Batched launches (one launch per kernel over the channels of a table).
+// Mode kernel: work items of `block` threads, a persistent grid of resident
+// blocks taking items from the counter pair `work` (zero before the first
+// launch; each launch leaves it zero).  variant -1 is the full-band solve.
+struct ModeBatchShape {
+  int block;  // threads per work item
+  bool quad;  // 4 threads per unique mode (else 2 per mode)
+  int grid;   // resident blocks on the device
+};
+ModeBatchShape modes_batch_shape(int variant);
+void launch_modes_batch(const BatchTable<ModeArgs> &t, int variant, int *work, int grid, cudaStream_t st);
+cudaError_t mean_batch_prepare(size_t smem_bytes);
+size_t mean_smem_bytes(int NY, int n_g);
+void launch_mean_batch(const BatchTable<MeanArgs> &t, bool smem, size_t smem_bytes, cudaStream_t st);
+void launch_advance_batch(const StepCounters &c, cudaStream_t st);
+int nl_batch_blocks(const NLArgs &a);
+void launch_nl_batch(const BatchTable<NLArgs> &t, cudaStream_t st);
+// Transforms: part 0 z backward, 1 x pass, 2 z forward, 3 mean-flow terms
+// (mixed precision).  The channels of a table share the precision, NZ2 (parts
+// 0, 2) or NX2 (part 1).
+int lamb_batch_blocks(const XformDims &d, int precision, int part);
+cudaError_t lamb_batch_prepare(const XformDims &d, int precision);
+void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st);
 
 }  // namespace owt

@@ -37,15 +37,18 @@ template <> struct XCfg<float> { static constexpr int TX = 12; static constexpr 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 
+// Each kernel's body takes its block coordinates explicitly: the one-channel
+// kernels pass blockIdx, the batched kernels the coordinates of the block
+// within its channel's grid.
 template <typename T>
-__global__ void __launch_bounds__(1024) k_zback(XformArgs a) {
+__device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, const int j, const int f) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
   const int ls = d.NZ2 + 1;
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + TX * ls;
-  const int i0 = blockIdx.x * TX, j = blockIdx.y, f = blockIdx.z;
+  const int i0 = bx * TX;
   const int M = d.NZ * d.NXH;
   const double2 *base = a.in[f];
   if (a.ring_mask & (1 << f)) base += (size_t)ring_head(*a.step) * a.fs;
@@ -69,14 +72,14 @@ __global__ void __launch_bounds__(1024) k_zback(XformArgs a) {
 }
 
 template <typename T, int P>
-__global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
+__device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
   const int ls = d.NX2 + 1;
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + 3 * P * ls;
   const size_t nlines = (size_t)d.NY * d.NZ2;
-  const size_t line0 = (size_t)blockIdx.x * P;
+  const size_t line0 = (size_t)bx * P;
   const size_t fstride = nlines * d.NXH;
   const cpx<T> *zb = reinterpret_cast<const cpx<T> *>(a.zbuf);
   // 1. pack field pairs (u,v), (w,ox), (oy,oz) into complex spectra; the
@@ -146,14 +149,14 @@ __global__ void __launch_bounds__(1024) k_xlamb(XformArgs a) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
+__device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, const int j, const int f) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
   const int ls = d.NZ2 + 1;
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + TX * ls;
-  const int i0 = blockIdx.x * TX, j = blockIdx.y, f = blockIdx.z;
+  const int i0 = bx * TX;
   const cpx<T> *src = reinterpret_cast<const cpx<T> *>(a.lbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
     const int z = idx / TX, c = idx - z * TX;
@@ -180,11 +183,11 @@ __global__ void __launch_bounds__(1024) k_zfwd(XformArgs a) {
 // Ubar, Obar are the real parts of the (0, 0) modes of row j; the kx = 0
 // column enters through its Hermitian part, as the real-part extraction of
 // the x transform makes it enter the physical product.  Grid: (modes / 256,
-// NY); one thread per mode of row blockIdx.y, all three components.
-__global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
+// NY); one thread per mode of row j (the grid's y), all three components.
+__device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx, const int j) {
   const XformDims d = a.d;
   const int M = d.NZ * d.NXH;
-  const int m = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  const int m = bx * 256 + threadIdx.x;
   if (m >= M) return;
   const int kz = m / d.NXH, kx = m - kz * d.NXH;
   if (kz == d.NZH) return;
@@ -242,6 +245,52 @@ __global__ void __launch_bounds__(256) k_mean_lamb(XformArgs a) {
       *o = make_double2(v.x + l.x, v.y + l.y);
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_zback(const __grid_constant__ XformArgs a) {
+  zback_body<T>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <typename T, int P>
+__global__ void __launch_bounds__(1024) k_xlamb(const __grid_constant__ XformArgs a) {
+  xlamb_body<T, P>(a, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(1024) k_zfwd(const __grid_constant__ XformArgs a) {
+  zfwd_body<T>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+__global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ XformArgs a) {
+  mean_lamb_body(a, blockIdx.x, blockIdx.y);
+}
+
+// Batched: one launch over every channel of a table whose channels share the
+// precision and the length of the lines a block spans (NZ2 for the z passes,
+// NX2 for the x pass); blocks are numbered channel by channel, each channel's
+// grid flattened x fastest.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_zback_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  const XformArgs &a = t.a[c];
+  const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
+  zback_body<T>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
+}
+template <typename T, int P>
+__global__ void __launch_bounds__(1024) k_xlamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  xlamb_body<T, P>(t.a[c], blockIdx.x - t.start[c]);
+}
+template <typename T>
+__global__ void __launch_bounds__(1024) k_zfwd_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  const XformArgs &a = t.a[c];
+  const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
+  zfwd_body<T>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
+}
+__global__ void __launch_bounds__(256) k_mean_lamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  const XformArgs &a = t.a[c];
+  const int gx = (a.d.NZ * a.d.NXH + 255) / 256, lb = blockIdx.x - t.start[c], r = lb / gx;
+  mean_lamb_body(a, lb - r * gx, r);
 }
 
 static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
@@ -331,6 +380,61 @@ static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_part_t<double>(a, part, st);
   else lamb_part_t<float>(a, part, st);
+}
+
+// Blocks of one channel in part 0 (z backward), 1 (x pass), 2 (z forward) or
+// 3 (mean-flow terms); the grids of the one-channel launches, flattened.
+template <typename T>
+static int lamb_blocks_t(const XformDims &d, int part) {
+  const int gx = (d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX;
+  if (part == 0) return gx * d.NY * 6;
+  if (part == 2) return gx * d.NY * 3;
+  if (part == 1) {
+    const int P = x_lines<T>(d);
+    return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
+  }
+  return ((d.NZ * d.NXH + 255) / 256) * d.NY;
+}
+int lamb_batch_blocks(const XformDims &d, int precision, int part) {
+  return precision == 0 ? lamb_blocks_t<double>(d, part) : lamb_blocks_t<float>(d, part);
+}
+
+template <typename T>
+static cudaError_t batch_prepare_t(const XformDims &d) {
+  const size_t sz = smem_z<T>(d);
+  cudaError_t e = raise_smem_limit(k_zback_batch<T>, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k_zfwd_batch<T>, sz);
+  if (e == cudaSuccess) {
+    if (x_lines<T>(d) == XCfg<T>::P) e = raise_smem_limit(k_xlamb_batch<T, XCfg<T>::P>, smem_x<T>(d, XCfg<T>::P));
+    else e = raise_smem_limit(k_xlamb_batch<T, 2>, smem_x<T>(d, 2));
+  }
+  return e;
+}
+cudaError_t lamb_batch_prepare(const XformDims &d, int precision) {
+  return precision == 0 ? batch_prepare_t<double>(d) : batch_prepare_t<float>(d);
+}
+
+template <typename T>
+static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t st) {
+  const XformDims &d = t.a[0].d;
+  const unsigned blocks = (unsigned)t.start[t.n];
+  if (part == 0) {
+    k_zback_batch<T><<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
+  } else if (part == 1) {
+    if (x_lines<T>(d) == XCfg<T>::P) {
+      k_xlamb_batch<T, XCfg<T>::P><<<blocks, d.NX2, smem_x<T>(d, XCfg<T>::P), st>>>(t);
+    } else {
+      k_xlamb_batch<T, 2><<<blocks, d.NX2, smem_x<T>(d, 2), st>>>(t);
+    }
+  } else if (part == 2) {
+    k_zfwd_batch<T><<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
+  } else {
+    k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
+  }
+}
+void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {
+  if (precision == 0) lamb_batch_t<double>(t, part, st);
+  else lamb_batch_t<float>(t, part, st);
 }
 
 size_t lamb_zbuf_bytes(const XformDims &d, int precision) {

@@ -1,4 +1,6 @@
-"""Many independent channels stepped together (one CUDA graph launch per step).
+"""Many independent channels stepped together: one CUDA graph launch per step,
+in which every kernel of the step covers all channels at once (the mode kernel
+as one persistent launch over every channel's banded solves).
 
 ``minimal_channels`` draws the uneven minimal-channel ensemble: Re_tau uniform
 in [150, 250] (bulk Reynolds number from Dean's correlation
@@ -62,6 +64,27 @@ class Batch:
         if rc != _L.OK:
             raise _L.OwtError(rc, "owt_batch_get_stream")
         return v.value
+
+    def _count(self, fn):
+        v = C.c_int64()
+        rc = fn(self.b, C.byref(v))
+        if rc != _L.OK:
+            raise _L.OwtError(rc, "batch launch count")
+        return v.value
+
+    @property
+    def launch_count(self):
+        """Kernels launched by this batch's steps (and its autotuner)."""
+        return self._count(self.L.owt_batch_get_launch_count)
+
+    @property
+    def step_launches(self):
+        """Kernels in one batch step."""
+        return self._count(self.L.owt_batch_get_step_launches)
+
+    def tuning_report(self):
+        """Timings of the mode-kernel variants on this batch, and the choice."""
+        return self.L.owt_batch_tuning_report(self.b).decode()
 
     def close(self):
         if getattr(self, "b", None):

@@ -79,6 +79,9 @@ def load(path=LIB):
         "owt_batch_synchronize": ([C.c_void_p], C.c_int),
         "owt_batch_destroy": ([C.c_void_p], C.c_int),
         "owt_batch_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+        "owt_batch_get_launch_count": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
+        "owt_batch_get_step_launches": ([C.c_void_p, C.POINTER(C.c_int64)], C.c_int),
+        "owt_batch_tuning_report": ([C.c_void_p], C.c_char_p),
         "owt_checkpoint_bytes": ([_h, C.POINTER(C.c_int64)], C.c_int),
         "owt_checkpoint_save": ([_h, C.c_void_p, C.c_int64], C.c_int),
         "owt_checkpoint_load": ([_h, C.c_void_p, C.c_int64], C.c_int),

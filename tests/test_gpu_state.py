@@ -119,6 +119,53 @@ def test_batch_step_matches_individual_steps(gpu_lib):
         for n in ("vely", "vory", "velx", "Hv", "lmbz"):
             np.testing.assert_array_equal(a.get(n), c.get(n))
         np.testing.assert_array_equal(a.friction(), c.friction())
+    # one graph launch of batched kernels: far fewer than one kernel set per channel
+    assert b.step_launches <= 12, b.step_launches
+    assert "->" in b.tuning_report()
+    b.close()
+
+
+def test_batch_of_66_mixed_channels_matches_individual_steps(gpu_lib):
+    """More channels than one launch table holds (64), FP64 and mixed-precision
+    channels, sixth-order channels (full-band solve), uneven sizes and one
+    channel with wall blowing/suction: every channel's bits equal stepping it
+    alone, and creating the batch (which times the mode-kernel variants on the
+    live state) leaves every channel's state untouched."""
+    from owt.adjoint import seeded_wall_field
+    from owt.batch import Batch
+    from owt.ic import seeded_velocity
+    from owt.params import CaseParams
+    from owt.solver import GpuSolver
+    sizes = [(16, 33, 16), (16, 17, 24), (24, 33, 16), (32, 25, 16)]
+    ps, precs = [], []
+    for q in range(66):
+        nx, ny, nz = sizes[q % 4]
+        ps.append(CaseParams(dt=0.004, dkx=0.5 + 0.01 * q, dkz=1.5, NX=nx, NY=ny, NZ=nz, alpha_mesh=2.0,
+                             nu=1 / 2800., fd_order=6 if q % 11 == 3 else 8))
+        precs.append("fp64" if q % 3 == 0 else "mixed")
+    alone, batched = [], []
+    for q, p in enumerate(ps):
+        for group in (alone, batched):
+            s = GpuSolver(p, precision=precs[q])
+            s.init_fields(*seeded_velocity(p, seed=q))
+            if q == 5:
+                s.set_wall_velocity(seeded_wall_field(p, 1), seeded_wall_field(p, 2))
+            group.append(s)
+    before = [(s.get("vely"), s.get("velx"), s.get("vory")) for s in batched]
+    b = Batch(batched)
+    b.synchronize()
+    for s, (v, u, g) in zip(batched, before):
+        np.testing.assert_array_equal(s.get("vely"), v)
+        np.testing.assert_array_equal(s.get("velx"), u)
+        np.testing.assert_array_equal(s.get("vory"), g)
+    b.step(2)
+    b.synchronize()
+    for s in alone:
+        s.time_Integration(2)
+    for q, (a, c) in enumerate(zip(alone, batched)):
+        for n in ("vely", "vory", "velx", "velz", "Hv", "Hg"):
+            np.testing.assert_array_equal(a.get(n), c.get(n), err_msg=f"channel {q} {n}")
+        np.testing.assert_array_equal(a.friction(), c.friction())
     b.close()
 
 
