@@ -410,11 +410,13 @@ def run_batch(args, rank, world, local_rank):
         dist.init_process_group("nccl")
     ps = minimal_channels(64, seed=0)
     solvers = []
+    t_setup = time.perf_counter()
     for q, p in enumerate(ps):
         s = GpuSolver(p, precision="mixed", device=local_rank)
         s.init_fields(*seeded_velocity(p, seed=q))
         s.use_graph(True)
         solvers.append(s)
+    t_setup = time.perf_counter() - t_setup
     points = sum(p.NX2 * p.NZ2 * p.NY for p in ps)
     # serial loop: one channel after another, each its own graph
     for s in solvers:
@@ -430,7 +432,9 @@ def run_batch(args, rank, world, local_rank):
     barrier()
     loop_ms, loop_rate = aggregate((time.perf_counter() - t0) * 1e3, 64 * k_loop, device="cuda")
     # batched: one graph launch per step, each kernel over all channels
+    t_batch = time.perf_counter()
     b = Batch(solvers)
+    t_batch = time.perf_counter() - t_batch
     b.step(args.warmup)
     b.synchronize()
     st = torch.cuda.ExternalStream(b.stream)
@@ -461,6 +465,7 @@ def run_batch(args, rank, world, local_rank):
         "config": {"workload": "batch64_minimal_channels", "precision": "mixed", "channels": 64,
                    "physical_points_total": points, "kernels_per_batch_step": step_launches,
                    "mode_kernel_autotune": tuning,
+                   "setup_s": {"channels_create_and_init": round(t_setup, 3), "batch_create": round(t_batch, 3)},
                    "l2": "no flush; per-step state of all channels ~%.1f GB" % (
                        sum(22 * 16 * p.NY * p.NZ * p.NXH for p in ps) / 1e9)},
         "variants": {"serial_loop": {"channel_steps_per_s": round(loop_rate, 3),
