@@ -234,6 +234,9 @@ int owt_state_restore(owt_handle *h);
 int owt_set_option(owt_handle *h, int option, int64_t value);
 int owt_get_info(const owt_handle *h, int what, int64_t *value);
 const char *owt_tuning_report(const owt_handle *h);
+/* Wall time of owt_create's phases (host operators, band factorizations,
+ * pattern check, fields and tables, mode-kernel autotune), as text. */
+const char *owt_setup_report(const owt_handle *h);
 
 /* Measurement aid, no counterpart in the reference: enqueue one stage of the
  * step on the handle's stream without advancing the step counter, so a caller

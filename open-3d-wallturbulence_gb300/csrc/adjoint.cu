@@ -87,6 +87,8 @@ void launch_adj_nl(const AdjNLArgs &a, cudaStream_t st) {
 // lines per z block, AP (y, z) lines per x block.
 constexpr int ATX = 6, AP = 2, ANPAIR = 5;
 
+// R5: the lines have a radix-5 stage (the butterfly is compiled in only then).
+template <bool R5>
 __global__ void __launch_bounds__(1024) k_zback_adj(AdjXformArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -113,7 +115,7 @@ __global__ void __launch_bounds__(1024) k_zback_adj(AdjXformArgs a) {
     }
   }
   __syncthreads();
-  const double2 *r = fft_lines<double, true>(bufa, bufb, ATX, ls, a.pz, a.twz);
+  const double2 *r = fft_lines<double, true, R5>(bufa, bufb, ATX, ls, a.pz, a.twz);
   double2 *dst = a.zbuf + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ2 * ATX; idx += blockDim.x) {
     const int z = idx / ATX, c = idx - z * ATX;
@@ -121,6 +123,7 @@ __global__ void __launch_bounds__(1024) k_zback_adj(AdjXformArgs a) {
   }
 }
 
+template <bool R5>
 __global__ void __launch_bounds__(1024) k_xlamb_adj(AdjXformArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(1024) k_xlamb_adj(AdjXformArgs a) {
     bufa[q * ls + mm] = z;
   }
   __syncthreads();
-  double2 *r = fft_lines<double, true>(bufa, bufb, ANPAIR * AP, ls, a.px, a.twx);
+  double2 *r = fft_lines<double, true, R5>(bufa, bufb, ANPAIR * AP, ls, a.px, a.twx);
   double2 *o = (r == bufa) ? bufb : bufa;
   // 2. u_bar = om x lb, om_bar = lb x u, packed (ub,vb) (wb,oxb) (oyb,ozb)
   for (int idx = threadIdx.x; idx < AP * d.NX2; idx += blockDim.x) {
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(1024) k_xlamb_adj(AdjXformArgs a) {
     o[(2 * AP + l) * ls + x] = make_double2(bz * u - bx * w, bx * v - by * u);
   }
   __syncthreads();
-  const double2 *fo = fft_lines<double, false>(o, r, 3 * AP, ls, a.px, a.twx);
+  const double2 *fo = fft_lines<double, false, R5>(o, r, 3 * AP, ls, a.px, a.twx);
   // 3. unpack the real-pair spectra, keep kx < NXH, weight 1 (kx = 0) or 2
   for (int idx = threadIdx.x; idx < AP * d.NXH; idx += blockDim.x) {
     const int l = idx / d.NXH, mm = idx - l * d.NXH;
@@ -186,6 +189,7 @@ __global__ void __launch_bounds__(1024) k_xlamb_adj(AdjXformArgs a) {
   }
 }
 
+template <bool R5>
 __global__ void __launch_bounds__(1024) k_zfwd_adj(AdjXformArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(1024) k_zfwd_adj(AdjXformArgs a) {
     bufa[c * ls + z] = (i0 + c < d.NXH) ? src[(size_t)z * d.NXH + i0 + c] : make_double2(0.0, 0.0);
   }
   __syncthreads();
-  const double2 *r = fft_lines<double, false>(bufa, bufb, ATX, ls, a.pz, a.twz);
+  const double2 *r = fft_lines<double, false, R5>(bufa, bufb, ATX, ls, a.pz, a.twz);
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ * ATX; idx += blockDim.x) {
     const int kz = idx / ATX, c = idx - kz * ATX;
@@ -215,21 +219,33 @@ static size_t adj_smem_x(const XformDims &d) { return 2 * (size_t)ANPAIR * AP * 
 size_t adj_zbuf_values(const XformDims &d) { return 9 * (size_t)d.NY * d.NZ2 * d.NXH; }
 size_t adj_lbuf_values(const XformDims &d) { return 6 * (size_t)d.NY * d.NZ2 * d.NXH; }
 
+// the instances for the channel's line lengths
+struct AdjXformKernels {
+  void (*zback)(AdjXformArgs), (*xlamb)(AdjXformArgs), (*zfwd)(AdjXformArgs);
+};
+static AdjXformKernels adj_kernels(const XformDims &d) {
+  const bool z5 = d.NZ2 % 5 == 0, x5 = d.NX2 % 5 == 0;
+  return {z5 ? k_zback_adj<true> : k_zback_adj<false>, x5 ? k_xlamb_adj<true> : k_xlamb_adj<false>,
+          z5 ? k_zfwd_adj<true> : k_zfwd_adj<false>};
+}
+
 cudaError_t adj_lamb_prepare(const XformDims &d) {
-  cudaError_t e = raise_smem_limit(k_zback_adj, adj_smem_z(d));
-  if (e == cudaSuccess) e = raise_smem_limit(k_zfwd_adj, adj_smem_z(d));
-  if (e == cudaSuccess) e = raise_smem_limit(k_xlamb_adj, adj_smem_x(d));
+  const AdjXformKernels k = adj_kernels(d);
+  cudaError_t e = raise_smem_limit(k.zback, adj_smem_z(d));
+  if (e == cudaSuccess) e = raise_smem_limit(k.zfwd, adj_smem_z(d));
+  if (e == cudaSuccess) e = raise_smem_limit(k.xlamb, adj_smem_x(d));
   return e;
 }
 
 void launch_adj_lamb(const AdjXformArgs &a, cudaStream_t st) {
   const XformDims &d = a.d;
+  const AdjXformKernels k = adj_kernels(d);
   dim3 gz((d.NXH + ATX - 1) / ATX, d.NY, 9);
-  k_zback_adj<<<gz, d.NZ2, adj_smem_z(d), st>>>(a);
+  k.zback<<<gz, d.NZ2, adj_smem_z(d), st>>>(a);
   const size_t nl = (size_t)d.NY * d.NZ2;
-  k_xlamb_adj<<<(unsigned)((nl + AP - 1) / AP), d.NX2, adj_smem_x(d), st>>>(a);
+  k.xlamb<<<(unsigned)((nl + AP - 1) / AP), d.NX2, adj_smem_x(d), st>>>(a);
   dim3 gf((d.NXH + ATX - 1) / ATX, d.NY, 6);
-  k_zfwd_adj<<<gf, d.NZ2, adj_smem_z(d), st>>>(a);
+  k.zfwd<<<gf, d.NZ2, adj_smem_z(d), st>>>(a);
 }
 
 // ---------------------------------------------------------------------------

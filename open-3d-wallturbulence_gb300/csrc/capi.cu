@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -148,7 +149,18 @@ struct owt_handle {
 
   // ---- setup -----------------------------------------------------------------
   size_t device_bytes = 0;
+  std::string setup_report;  // wall time of the setup phases
   void setup(const owt_params &prm) {
+    using clk = std::chrono::steady_clock;
+    auto t_last = clk::now();
+    auto phase = [&](const char *name) {
+      const auto t = clk::now();
+      char buf[64];
+      std::snprintf(buf, sizeof(buf), "%s%s %.2fms", setup_report.empty() ? "" : ", ", name,
+                    std::chrono::duration<double, std::milli>(t - t_last).count());
+      setup_report += buf;
+      t_last = t;
+    };
     g_alloc_counter = &device_bytes;
     struct Reset { ~Reset() { g_alloc_counter = nullptr; } } reset_counter;
     p = prm;
@@ -169,7 +181,7 @@ struct owt_handle {
     precision = p.precision;
     std::vector<int> rx, rz;
     if (!fft_radices(NX2, rx) || !fft_radices(NZ2, rz))
-      throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must be of the form 2^a 3^b");
+      throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must be of the form 2^a 3^b 5^c");
     if (NX2 > 1024 || NZ2 > 1024)
       throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must not exceed 1024 (one thread per point of a line)");
     px.L = NX2; px.nst = (int)rx.size();
@@ -236,6 +248,8 @@ struct owt_handle {
     ck(cudaMemsetAsync(d_step, 0, sizeof(long long), st), "memset");
     ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "memset");
 
+    ck(cudaStreamSynchronize(st), "setup");
+    phase("host operators");
     // band factorizations
     double *d_sa = upload(sa, owned, st), *d_sb = upload(sb, owned, st), *d_icg = inv_cg;
     auto factor = [&](BandDev &bd, const BandTemplate &t, int U, const double *s1, const double *s2, bool rows) {
@@ -259,6 +273,7 @@ struct owt_handle {
     int herr = 0;
     ck(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost), "factor status");
     if (herr) throw OwtError(OWT_ERR_NUMERIC, "LU factorization failed. Matrix A may be singular.");
+    phase("band factorizations");
     // interior fill of both systems inside the compile-time masks? then the
     // masked solves apply
     sparse_v = false;
@@ -275,6 +290,7 @@ struct owt_handle {
       sparse_v = (nbad[0] == 0 && nbad[1] == 0);
       pattern_violations = nbad[0] + nbad[1];
     }
+    phase("pattern check");
     rhs_node_v = upload(tv.rhs_node, owned, st);
     rbv_col = upload(tv.rbv_col, owned, st);
     rbv_val = upload(tv.rbv_val, owned, st);
@@ -360,7 +376,8 @@ struct owt_handle {
     for (double2 *f : {u, w, ox, oz, lx, ly, lz})
       ck(cudaMemsetAsync(f, 0, fs * sizeof(double2), st), "memset");
     ck(cudaStreamSynchronize(st), "setup");
-    autotune_modes();
+    phase("fields and tables");
+    tuning = "not tuned yet (the variants are timed before the handle's first own step)";
   }
 
   // ---- kernel sequences --------------------------------------------------------
@@ -463,6 +480,7 @@ struct owt_handle {
   }
 
   void run_steps(int64_t n) {
+    ensure_tuned();
     recompute_dirty_q();
     if (use_graph) {
       if (!gexec) {
@@ -495,9 +513,39 @@ struct owt_handle {
   int forced_variant = -1;   // testing aid: run this variant instead
   std::string tuning;        // autotuner report
 
-  // Autotuner: time every mode-kernel variant on the (zero) state, keep the
-  // fastest.  Variants differ only in thread mapping and block shape; their
-  // results are bitwise identical, so the choice affects speed only.
+  // Autotuner: time every mode-kernel variant, keep the fastest.  Variants
+  // differ only in thread mapping and block shape; their results are bitwise
+  // identical, so the choice affects speed only.  It runs once, before the
+  // handle's first own step (a handle stepped only inside a batch never needs
+  // it); on a live state the rings and fields the trials overwrite are copied
+  // aside and put back.
+  bool tuned = false;
+  void ensure_tuned() {
+    if (tuned) return;
+    tuned = true;
+    if (!initialized) {
+      autotune_modes();
+      return;
+    }
+    recompute_dirty_q();
+    double2 *snap = nullptr;
+    ck(cudaMalloc(&snap, 13 * fs * sizeof(double2)), "tuning snapshot");
+    try {
+      double2 *o = snap;
+      for (double2 *ring : {v_ring, g_ring, q_ring}) { d2d(o, ring, 3 * fs * sizeof(double2)); o += 3 * fs; }
+      for (double2 *f : {u, w, ox, oz}) { d2d(o, f, fs * sizeof(double2)); o += fs; }
+      autotune_modes();
+      o = snap;
+      for (double2 *ring : {v_ring, g_ring, q_ring}) { d2d(ring, o, 3 * fs * sizeof(double2)); o += 3 * fs; }
+      for (double2 *f : {u, w, ox, oz}) { d2d(f, o, fs * sizeof(double2)); o += fs; }
+      ck(cudaStreamSynchronize(st), "tuning restore");
+    } catch (...) {
+      cudaStreamSynchronize(st);
+      cudaFree(snap);
+      throw;
+    }
+    cudaFree(snap);
+  }
   void autotune_modes() {
     modes_variant = 0;
     tuning.clear();
@@ -1559,6 +1607,7 @@ int owt_set_option(owt_handle *h, int option, int64_t value) {
 }
 
 const char *owt_tuning_report(const owt_handle *h) { return h ? h->tuning.c_str() : ""; }
+const char *owt_setup_report(const owt_handle *h) { return h ? h->setup_report.c_str() : ""; }
 
 int owt_get_info(const owt_handle *h, int what, int64_t *value) {
   if (!h || !value) return OWT_ERR_INVALID;
@@ -1576,7 +1625,7 @@ int owt_enqueue_stage(owt_handle *h, int stage) {
   return guard(h, [&] {
     if (!h->initialized) throw OwtError(OWT_ERR_STATE, "owt_init_fields must come first");
     switch (stage) {
-      case OWT_STAGE_MODES: h->stage_modes(); h->launches += 1; break;
+      case OWT_STAGE_MODES: h->ensure_tuned(); h->stage_modes(); h->launches += 1; break;
       case OWT_STAGE_MEAN: h->stage_mean(); h->launches += 1; break;
       case OWT_STAGE_LAMB: h->launches += launch_lamb(h->xform_args(), h->precision, h->st); break;
       case OWT_STAGE_NONLINEAR: launch_nl(h->nl_args(true), h->st); h->launches += 1; break;

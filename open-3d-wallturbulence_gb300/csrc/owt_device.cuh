@@ -35,7 +35,7 @@ template <> __device__ __forceinline__ float2 from_d<float>(double2 a) { return 
 
 // ---------------------------------------------------------------------------
 // FFT of many lines held in shared memory: self-sorting (Stockham) mixed-radix
-// schedule with radices 4, 2, 3.  At a stage of radix R after ns points have
+// schedule with radices 4, 2, 3, 5.  At a stage of radix R after ns points have
 // been combined, butterfly j (of L/R) reads x[j + r L/R], multiplies by
 // w^(k r) with k = j mod ns and w = exp(sign 2 pi i / (ns R)), transforms, and
 // writes y[(j / ns) ns R + k + r ns].  Twiddles come from one table of
@@ -55,9 +55,9 @@ __device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx
   return w;
 }
 
-template <typename T, bool BACKWARD>
+template <typename T, bool BACKWARD, bool R5>
 __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R, int j, int nr, int ns, int base,
-                                          cpx<T> w1, cpx<T> w2, cpx<T> w3, bool twid) {
+                                          cpx<T> w1, cpx<T> w2, cpx<T> w3, cpx<T> w4, bool twid) {
   if (R == 4) {
     cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
     if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); }
@@ -74,6 +74,28 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
     if (twid) x1 = cmul(x1, w1);
     dst[base] = cadd(x0, x1);
     dst[base + ns] = csub(x0, x1);
+  } else if (R5 && R == 5) {
+    // DFT of length 5 from the sums and differences of the pairs (1, 4) and
+    // (2, 3): y1,4 = a1 -+ sign i b1 and y2,3 = a2 -+ sign i b2 with
+    // a1 = x0 + c1 t1 + c2 t2, a2 = x0 + c2 t1 + c1 t2,
+    // b1 = s1 d1 + s2 d2, b2 = s2 d1 - s1 d2 (c_n, s_n = cos, sin 2 pi n / 5)
+    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr], x4 = src[j + 4 * nr];
+    if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); x4 = cmul(x4, w4); }
+    const T c1 = (T)0.30901699437494742410229341718281906, c2 = (T)-0.80901699437494742410229341718281906;
+    const T s1 = (T)0.95105651629515357211643933337938214, s2 = (T)0.58778525229247312916870595463907277;
+    const cpx<T> t1 = cadd(x1, x4), t2 = cadd(x2, x3), d1 = csub(x1, x4), d2 = csub(x2, x3);
+    const cpx<T> a1 = mk<T>(x0.x + c1 * t1.x + c2 * t2.x, x0.y + c1 * t1.y + c2 * t2.y);
+    const cpx<T> a2 = mk<T>(x0.x + c2 * t1.x + c1 * t2.x, x0.y + c2 * t1.y + c1 * t2.y);
+    const cpx<T> b1 = mk<T>(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y);
+    const cpx<T> b2 = mk<T>(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y);
+    // e = b * (-sign i): forward (-i) b = (b.y, -b.x), backward (+i) b = (-b.y, b.x)
+    const cpx<T> e1 = BACKWARD ? mk<T>(-b1.y, b1.x) : mk<T>(b1.y, -b1.x);
+    const cpx<T> e2 = BACKWARD ? mk<T>(-b2.y, b2.x) : mk<T>(b2.y, -b2.x);
+    dst[base] = cadd(x0, cadd(t1, t2));
+    dst[base + ns] = cadd(a1, e1);
+    dst[base + 2 * ns] = cadd(a2, e2);
+    dst[base + 3 * ns] = csub(a2, e2);
+    dst[base + 4 * ns] = csub(a1, e1);
   } else {  // R == 3
     cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
     if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); }
@@ -94,7 +116,8 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
 // and applies it to every (blockDim / (L/R))-th line, so index arithmetic and
 // twiddle loads happen once per stage; a block of L threads keeps every thread
 // busy for radix 2, 3 and 4 when nlines is a multiple of 12.
-template <typename T, bool BACKWARD>
+// R5 compiles in the radix-5 butterfly; a plan with a radix-5 stage needs it.
+template <typename T, bool BACKWARD, bool R5>
 __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, const FftPlan &p,
                              const cpx<T> *__restrict__ tw) {
   const int L = p.L;
@@ -111,27 +134,29 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
         const int k = j % ns;
         const int base = (j - k) * R + k;
         const bool twid = k != 0;
-        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1;
+        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1, w4 = w1;
         if (twid) {
           w1 = twiddle<T, BACKWARD>(tw, k * step);
           if (R >= 3) w2 = twiddle<T, BACKWARD>(tw, 2 * k * step);
-          if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
+          if (R >= 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
+          if (R5 && R == 5) w4 = twiddle<T, BACKWARD>(tw, 4 * k * step);
         }
         for (int line = lo; line < nlines; line += per)
-          butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, base, w1, w2, w3, twid);
+          butterfly<T, BACKWARD, R5>(a + line * lstride, b + line * lstride, R, j, nr, ns, base, w1, w2, w3, w4, twid);
       }
     } else {
       for (int idx = tid; idx < nlines * nr; idx += nt) {
         const int line = idx / nr, j = idx - line * nr;
         const int k = j % ns;
         const bool twid = k != 0;
-        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1;
+        cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1, w4 = w1;
         if (twid) {
           w1 = twiddle<T, BACKWARD>(tw, k * step);
           if (R >= 3) w2 = twiddle<T, BACKWARD>(tw, 2 * k * step);
-          if (R == 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
+          if (R >= 4) w3 = twiddle<T, BACKWARD>(tw, 3 * k * step);
+          if (R5 && R == 5) w4 = twiddle<T, BACKWARD>(tw, 4 * k * step);
         }
-        butterfly<T, BACKWARD>(a + line * lstride, b + line * lstride, R, j, nr, ns, (j - k) * R + k, w1, w2, w3,
+        butterfly<T, BACKWARD, R5>(a + line * lstride, b + line * lstride, R, j, nr, ns, (j - k) * R + k, w1, w2, w3, w4,
                                twid);
       }
     }

@@ -40,7 +40,7 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 // Each kernel's body takes its block coordinates explicitly: the one-channel
 // kernels pass blockIdx, the batched kernels the coordinates of the block
 // within its channel's grid.
-template <typename T>
+template <typename T, bool R5>
 __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, const int j, const int f) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -63,7 +63,7 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
     }
   }
   __syncthreads();
-  const cpx<T> *r = fft_lines<T, true>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
+  const cpx<T> *r = fft_lines<T, true, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   cpx<T> *dst = reinterpret_cast<cpx<T> *>(a.zbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
     const int z = idx / TX, c = idx - z * TX;
@@ -71,7 +71,7 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
   }
 }
 
-template <typename T, int P>
+template <typename T, int P, bool R5>
 __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
@@ -108,7 +108,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   }
   __syncthreads();
   const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.twx);
-  cpx<T> *r = fft_lines<T, true>(bufa, bufb, 3 * P, ls, a.px, tw);
+  cpx<T> *r = fft_lines<T, true, R5>(bufa, bufb, 3 * P, ls, a.px, tw);
   cpx<T> *o = (r == bufa) ? bufb : bufa;
   // 2. lamb = u x omega, packed as (lx + i ly) per line and (lz_l + i lz_l+1)
 #pragma unroll
@@ -124,7 +124,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
     else o[(P + l / 2) * ls + x].x = lz;
   }
   __syncthreads();
-  cpx<T> *fo = fft_lines<T, false>(o, r, P + P / 2, ls, a.px, tw);
+  cpx<T> *fo = fft_lines<T, false, R5>(o, r, P + P / 2, ls, a.px, tw);
   // 3. unpack the real-pair spectra, keep kx < NXH, scale by 1/NX2
   cpx<T> *lb = reinterpret_cast<cpx<T> *>(a.lbuf);
   const T half = (T)(0.5 * a.inv_nx2);
@@ -148,7 +148,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   }
 }
 
-template <typename T>
+template <typename T, bool R5>
 __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, const int j, const int f) {
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -163,7 +163,7 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
     bufa[c * ls + z] = (i0 + c < d.NXH) ? src[(size_t)z * d.NXH + i0 + c] : mk<T>((T)0, (T)0);
   }
   __syncthreads();
-  const cpx<T> *r = fft_lines<T, false>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
+  const cpx<T> *r = fft_lines<T, false, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
   const double sc = a.inv_nz2;
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
@@ -247,17 +247,20 @@ __device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx,
   }
 }
 
-template <typename T>
+// Kernels.  R5: the lines the kernel transforms have a radix-5 stage (3NZ/2,
+// 3NX/2 divisible by 5).  The radix-5 butterfly is compiled only into those
+// instances, so the others keep their register budget (and occupancy).
+template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zback(const __grid_constant__ XformArgs a) {
-  zback_body<T>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+  zback_body<T, R5>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-template <typename T, int P>
+template <typename T, int P, bool R5>
 __global__ void __launch_bounds__(1024) k_xlamb(const __grid_constant__ XformArgs a) {
-  xlamb_body<T, P>(a, blockIdx.x);
+  xlamb_body<T, P, R5>(a, blockIdx.x);
 }
-template <typename T>
+template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zfwd(const __grid_constant__ XformArgs a) {
-  zfwd_body<T>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+  zfwd_body<T, R5>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 __global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ XformArgs a) {
   mean_lamb_body(a, blockIdx.x, blockIdx.y);
@@ -267,24 +270,24 @@ __global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ Xform
 // precision and the length of the lines a block spans (NZ2 for the z passes,
 // NX2 for the x pass); blocks are numbered channel by channel, each channel's
 // grid flattened x fastest.
-template <typename T>
+template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zback_batch(const __grid_constant__ BatchTable<XformArgs> t) {
   const int c = batch_channel(t.start, t.n, blockIdx.x);
   const XformArgs &a = t.a[c];
   const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
-  zback_body<T>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
+  zback_body<T, R5>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
 }
-template <typename T, int P>
+template <typename T, int P, bool R5>
 __global__ void __launch_bounds__(1024) k_xlamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
   const int c = batch_channel(t.start, t.n, blockIdx.x);
-  xlamb_body<T, P>(t.a[c], blockIdx.x - t.start[c]);
+  xlamb_body<T, P, R5>(t.a[c], blockIdx.x - t.start[c]);
 }
-template <typename T>
+template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zfwd_batch(const __grid_constant__ BatchTable<XformArgs> t) {
   const int c = batch_channel(t.start, t.n, blockIdx.x);
   const XformArgs &a = t.a[c];
   const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
-  zfwd_body<T>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
+  zfwd_body<T, R5>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
 }
 __global__ void __launch_bounds__(256) k_mean_lamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
   const int c = batch_channel(t.start, t.n, blockIdx.x);
@@ -308,49 +311,76 @@ template <typename T>
 static int x_lines(const XformDims &d) {
   return smem_x<T>(d, XCfg<T>::P) <= 227 * 1024 ? XCfg<T>::P : 2;
 }
+
+// The instances a channel's transforms use: by precision, x lines per block
+// and radix-5 stages of the z and x lines.
 template <typename T>
-static void launch_x(const XformArgs &a, cudaStream_t st) {
-  const XformDims &d = a.d;
-  const size_t nl = (size_t)d.NY * d.NZ2;
-  if (x_lines<T>(d) == XCfg<T>::P) {
-    constexpr int P = XCfg<T>::P;
-    k_xlamb<T, P><<<(unsigned)((nl + P - 1) / P), d.NX2, smem_x<T>(d, P), st>>>(a);
+struct XformKernels {
+  int P;
+  void (*zback)(XformArgs), (*xlamb)(XformArgs), (*zfwd)(XformArgs);
+  void (*zback_b)(BatchTable<XformArgs>), (*xlamb_b)(BatchTable<XformArgs>), (*zfwd_b)(BatchTable<XformArgs>);
+};
+template <typename T>
+static XformKernels<T> kernels(const XformDims &d) {
+  constexpr int PP = XCfg<T>::P;
+  const bool z5 = d.NZ2 % 5 == 0, x5 = d.NX2 % 5 == 0;
+  XformKernels<T> k;
+  k.P = x_lines<T>(d);
+  k.zback = z5 ? k_zback<T, true> : k_zback<T, false>;
+  k.zfwd = z5 ? k_zfwd<T, true> : k_zfwd<T, false>;
+  k.zback_b = z5 ? k_zback_batch<T, true> : k_zback_batch<T, false>;
+  k.zfwd_b = z5 ? k_zfwd_batch<T, true> : k_zfwd_batch<T, false>;
+  if (k.P == PP) {
+    k.xlamb = x5 ? k_xlamb<T, PP, true> : k_xlamb<T, PP, false>;
+    k.xlamb_b = x5 ? k_xlamb_batch<T, PP, true> : k_xlamb_batch<T, PP, false>;
   } else {
-    k_xlamb<T, 2><<<(unsigned)((nl + 1) / 2), d.NX2, smem_x<T>(d, 2), st>>>(a);
+    k.xlamb = x5 ? k_xlamb<T, 2, true> : k_xlamb<T, 2, false>;
+    k.xlamb_b = x5 ? k_xlamb_batch<T, 2, true> : k_xlamb_batch<T, 2, false>;
+  }
+  return k;
+}
+
+// One of the kernels (0: z backward, 1: x pass, 2: z forward, 3: the
+// mean-flow term of the mixed-precision Lamb vector).
+template <typename T>
+static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
+  const XformDims &d = a.d;
+  const XformKernels<T> k = kernels<T>(d);
+  constexpr int TX = XCfg<T>::TX;
+  const size_t sz = smem_z<T>(d);
+  if (part == 0) {
+    k.zback<<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), d.NZ2, sz, st>>>(a);
+  } else if (part == 1) {
+    const size_t nl = (size_t)d.NY * d.NZ2;
+    k.xlamb<<<(unsigned)((nl + k.P - 1) / k.P), d.NX2, smem_x<T>(d, k.P), st>>>(a);
+  } else if (part == 2) {
+    k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
+  } else if (a.mean_split) {
+    launch_mean_lamb(a, st);
   }
 }
 
 template <typename T>
 static int lamb_t(const XformArgs &a, cudaStream_t st) {
-  const XformDims &d = a.d;
-  constexpr int TX = XCfg<T>::TX;
-  const size_t sz = smem_z<T>(d);
-  dim3 gz((d.NXH + TX - 1) / TX, d.NY, 6);
-  k_zback<T><<<gz, d.NZ2, sz, st>>>(a);
-  launch_x<T>(a, st);
-  dim3 gf((d.NXH + TX - 1) / TX, d.NY, 3);
-  k_zfwd<T><<<gf, d.NZ2, sz, st>>>(a);
-  if (a.mean_split) {
-    launch_mean_lamb(a, st);
-    return 4;
-  }
-  return 3;
+  for (int part = 0; part < 4; ++part) lamb_part_t<T>(a, part, st);
+  return a.mean_split ? 4 : 3;
 }
 
+// Opt the channel's transform kernels (single and batched) in to the dynamic
+// shared memory they need, before any launch or graph capture.
 template <typename T>
 static cudaError_t prepare_t(const XformDims &d) {
-  const size_t sz = smem_z<T>(d);
-  cudaError_t e = raise_smem_limit(k_zback<T>, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k_zfwd<T>, sz);
-  if (e == cudaSuccess) {
-    if (x_lines<T>(d) == XCfg<T>::P) e = raise_smem_limit(k_xlamb<T, XCfg<T>::P>, smem_x<T>(d, XCfg<T>::P));
-    else e = raise_smem_limit(k_xlamb<T, 2>, smem_x<T>(d, 2));
-  }
+  const XformKernels<T> k = kernels<T>(d);
+  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d, k.P);
+  cudaError_t e = raise_smem_limit(k.zback, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k.zfwd, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k.xlamb, sx);
+  if (e == cudaSuccess) e = raise_smem_limit(k.zback_b, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k.zfwd_b, sz);
+  if (e == cudaSuccess) e = raise_smem_limit(k.xlamb_b, sx);
   return e;
 }
 
-// Opt the transform kernels in to the dynamic shared memory they need; called
-// once per handle, before any launch or graph capture.
 cudaError_t lamb_prepare(const XformDims &d) {
   cudaError_t e = prepare_t<double>(d);
   return e == cudaSuccess ? prepare_t<float>(d) : e;
@@ -360,23 +390,6 @@ int launch_lamb(const XformArgs &a, int precision, cudaStream_t st) {
   return precision == 0 ? lamb_t<double>(a, st) : lamb_t<float>(a, st);
 }
 
-// One of the kernels alone (0: z backward, 1: x pass, 2: z forward, 3: the
-// mean-flow term of the mixed-precision Lamb vector), for timing.
-template <typename T>
-static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
-  const XformDims &d = a.d;
-  constexpr int TX = XCfg<T>::TX;
-  const size_t sz = smem_z<T>(d);
-  if (part == 0) {
-    k_zback<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), d.NZ2, sz, st>>>(a);
-  } else if (part == 1) {
-    launch_x<T>(a, st);
-  } else if (part == 2) {
-    k_zfwd<T><<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
-  } else if (a.mean_split) {
-    launch_mean_lamb(a, st);
-  }
-}
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_part_t<double>(a, part, st);
   else lamb_part_t<float>(a, part, st);
@@ -399,38 +412,19 @@ int lamb_batch_blocks(const XformDims &d, int precision, int part) {
   return precision == 0 ? lamb_blocks_t<double>(d, part) : lamb_blocks_t<float>(d, part);
 }
 
-template <typename T>
-static cudaError_t batch_prepare_t(const XformDims &d) {
-  const size_t sz = smem_z<T>(d);
-  cudaError_t e = raise_smem_limit(k_zback_batch<T>, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k_zfwd_batch<T>, sz);
-  if (e == cudaSuccess) {
-    if (x_lines<T>(d) == XCfg<T>::P) e = raise_smem_limit(k_xlamb_batch<T, XCfg<T>::P>, smem_x<T>(d, XCfg<T>::P));
-    else e = raise_smem_limit(k_xlamb_batch<T, 2>, smem_x<T>(d, 2));
-  }
-  return e;
-}
 cudaError_t lamb_batch_prepare(const XformDims &d, int precision) {
-  return precision == 0 ? batch_prepare_t<double>(d) : batch_prepare_t<float>(d);
+  return precision == 0 ? prepare_t<double>(d) : prepare_t<float>(d);
 }
 
 template <typename T>
 static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t st) {
   const XformDims &d = t.a[0].d;
+  const XformKernels<T> k = kernels<T>(d);
   const unsigned blocks = (unsigned)t.start[t.n];
-  if (part == 0) {
-    k_zback_batch<T><<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
-  } else if (part == 1) {
-    if (x_lines<T>(d) == XCfg<T>::P) {
-      k_xlamb_batch<T, XCfg<T>::P><<<blocks, d.NX2, smem_x<T>(d, XCfg<T>::P), st>>>(t);
-    } else {
-      k_xlamb_batch<T, 2><<<blocks, d.NX2, smem_x<T>(d, 2), st>>>(t);
-    }
-  } else if (part == 2) {
-    k_zfwd_batch<T><<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
-  } else {
-    k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
-  }
+  if (part == 0) k.zback_b<<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
+  else if (part == 1) k.xlamb_b<<<blocks, d.NX2, smem_x<T>(d, k.P), st>>>(t);
+  else if (part == 2) k.zfwd_b<<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
+  else k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
 }
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_batch_t<double>(t, part, st);

@@ -73,6 +73,7 @@ def load(path=LIB):
         "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),
         "owt_get_info": ([_h, C.c_int, C.POINTER(C.c_int64)], C.c_int),
         "owt_tuning_report": ([_h], C.c_char_p),
+        "owt_setup_report": ([_h], C.c_char_p),
         "owt_statistics": ([_h, _dp], C.c_int),
         "owt_batch_create": ([C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)], C.c_int),
         "owt_batch_step": ([C.c_void_p, C.c_int64], C.c_int),

@@ -180,6 +180,10 @@ class GpuSolver:
     def tuning_report(self):
         return self.L.owt_tuning_report(self.h).decode()
 
+    def setup_report(self):
+        """Wall time of the setup phases of this handle's creation."""
+        return self.L.owt_setup_report(self.h).decode()
+
     def info(self, what):
         codes = {"sparse_solve": 1, "pattern_violations": 2, "device_bytes": 3, "modes_variant": 4,
                  "modes_variants": 5}

@@ -37,7 +37,7 @@ def _params(**kw):
 
 @pytest.mark.parametrize("bad,msg", [
     (dict(NX=15), "even"), (dict(NY=5), "at least 7"), (dict(dt=-1.0), "positive"),
-    (dict(precision=7), "precision"), (dict(NX=20), "2^a 3^b"),
+    (dict(precision=7), "precision"), (dict(NX=28), "2^a 3^b 5^c"),
 ])
 def test_create_rejects_bad_parameters_without_a_gpu(gpu_lib, bad, msg):
     from owt import lib as L

@@ -347,3 +347,137 @@ def test_long_x_lines_step_matches_oracle(gpu_lib, port_lib):
         g.time_Integration(1)
         o.step(1)
         compare_state(g, o, 1e-10, tag=f"NX=512 step{s + 1}")
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(20, 21, 40), (40, 16, 20)])
+def test_radix5_lines_step_matches_oracle(gpu_lib, port_lib, nx, ny, nz):
+    """Line lengths with a factor 5 (3NX/2, 3NZ/2 = 30, 60: radix-5 FFT stages)
+    and an even NY, the shapes of the reference's own cases, in FP64."""
+    from owt.ic import seeded_velocity
+    from owt.params import CaseParams
+    p = CaseParams(dt=0.004, dkx=0.5, dkz=1.0, NX=nx, NY=ny, NZ=nz, alpha_mesh=2.0, nu=1 / 2800.)
+    u, v, w = seeded_velocity(p, seed=5)
+    g, o = gpu_solver(p), port(p)
+    g.init_fields(u, v, w)
+    o.set_velocity(u, v, w)
+    compare_state(g, o, 1e-12, tag=f"{nx}x{ny}x{nz} init")
+    for s in range(3):
+        g.time_Integration(1)
+        o.step(1)
+        compare_state(g, o, 1e-10, tag=f"{nx}x{ny}x{nz} step{s + 1}")
+
+
+def test_reference_retau180_case_size_step_matches_oracle(gpu_lib, port_lib):
+    """The reference's own Re_tau=180 case (test-cases/Retau-180/case.toml:
+    nu 3.5714e-4, dt 2e-3, dkx 0.25, dkz 0.5, 320 x 160 x 320, alpha 2.0):
+    physical lines of 480 points (2^5 3 5).  One FP64 step against the oracle
+    within the 128x129x128 bound, and the mixed-precision step's relative
+    deviation from it stated and bounded."""
+    from owt.ic import seeded_velocity
+    from owt.params import CaseParams
+    p = CaseParams(dt=2.0e-3, dkx=0.25, dkz=0.5, NX=320, NY=160, NZ=320, alpha_mesh=2.0,
+                   nu=3.571428571428571e-4)
+    u, v, w = seeded_velocity(p, seed=0)
+    g, o = gpu_solver(p), port(p)
+    o.set_threads(0)
+    g.init_fields(u, v, w)
+    o.set_velocity(u, v, w)
+    g.time_Integration(1)
+    o.step(1)
+    compare_state(g, o, 1e-8, fields=CURRENT, tag="Retau-180 case step1")
+    m = gpu_solver(p, precision="mixed")
+    m.init_fields(u, v, w)
+    m.time_Integration(1)
+    dev = {n: rel(m.get(n), g.get(n)) for n in ("vely", "vory", "Hv", "Hg", "lmbx", "lmby", "lmbz")}
+    print("Retau-180 case, mixed vs FP64 after one step:", {k: f"{v:.1e}" for k, v in dev.items()})
+    assert dev["vely"] < 1e-6 and dev["vory"] < 1e-6 and dev["lmbx"] < 1e-5
+
+
+def _np_lamb_planes(u, v, w, ox, oy, oz, NZ, NXH, NX2, NZ2, planes):
+    """The dealiased Lamb vector (src/solver.cpp:262-304 with the transforms of
+    src/FFT.cpp:49-194) on single y planes, by numpy's FFT."""
+    NZH = NZ // 2
+
+    def to_phys(f):
+        P = np.zeros((NZ2, NXH), np.complex128)
+        P[:NZH] = f[:NZH]
+        P[NZ2 - NZ + NZH + 1:] = f[NZH + 1:]  # Nyquist row dropped
+        Pz = np.fft.ifft(P, axis=0, norm="forward")
+        X = np.zeros((NZ2, NX2), np.complex128)
+        X[:, :NXH] = Pz
+        X[:, NX2 - NXH + 1:] = np.conj(Pz[:, 1:NXH][:, ::-1])
+        return np.fft.ifft(X, axis=1, norm="forward").real
+
+    def to_spec(p):
+        X = np.fft.fft(p, axis=1)[:, :NXH] / NX2
+        Z = np.fft.fft(X, axis=0)
+        return np.concatenate([Z[:NZH], Z[NZ:NZ2]], axis=0) / NZ2
+
+    out = []
+    for j in planes:
+        U, V, W = (to_phys(f[:, :, j]) for f in (u, v, w))
+        OX, OY, OZ = (to_phys(f[:, :, j]) for f in (ox, oy, oz))
+        out.append((to_spec(V * OZ - W * OY), to_spec(W * OX - U * OZ), to_spec(U * OY - V * OX)))
+    return out
+
+
+def test_reference_retau550_case_size_lamb_vector_and_steps(gpu_lib):
+    """The reference's own Re_tau=550 case (test-cases/Retau-550/case.toml:
+    nu 1e-4, dt 1e-3, dkx 0.5, dkz 1.0, 640 x 288 x 640, alpha 2.4): physical
+    lines of 960 points (2^6 3 5), the FP64 x pass at two lines per block.
+    The Lamb vector from init_fields on four y planes against numpy's FFT
+    (max-norm relative 1e-12), the mixed-precision Lamb vector against it
+    (relative L2 1e-6, the one-step RHS bound), and two steps of each that
+    stay finite."""
+    from owt.params import CaseParams
+    p = CaseParams(dt=1.0e-3, dkx=0.5, dkz=1.0, NX=640, NY=288, NZ=640, alpha_mesh=2.4, nu=1.0e-4)
+    NZ, NXH, NY = p.spectral_shape
+    rng = np.random.default_rng(3)
+    kx = np.arange(NXH) * p.dkx
+    kz = np.where(np.arange(NZ) < p.NZH, np.arange(NZ), np.arange(NZ) - NZ) * p.dkz
+    K = np.sqrt(kx[None, :] ** 2 + kz[:, None] ** 2)
+    amp = np.where(K > 0, (np.maximum(K, 1e-300) / 0.5) ** -2.0, 0.0) * 0.05
+    y = np.tanh(p.alpha_mesh * np.linspace(-1, 1, NY)) / np.tanh(p.alpha_mesh)
+    shape = (1 - y ** 2)
+
+    def field():
+        f = (rng.standard_normal((NZ, NXH, NY)) + 1j * rng.standard_normal((NZ, NXH, NY)))
+        f *= amp[:, :, None]
+        f *= shape[None, None, :]
+        f[p.NZH] = 0.0
+        f[NZ - np.arange(1, p.NZH), 0] = np.conj(f[np.arange(1, p.NZH), 0])
+        f[0, 0] = 0.0
+        return f
+
+    u, v, w = field(), field() * shape[None, None, :], field()
+    u[0, 0] = 1.5 * (1 - y ** 2)
+    g = gpu_solver(p)
+    g.init_fields(u, v, w)
+    planes = [0, 1, 143, NY - 1]
+    want = _np_lamb_planes(u, v, w, g.get("vorx"), g.get("vory"), g.get("vorz"), NZ, NXH, p.NX2, p.NZ2, planes)
+    got = [g.get(n) for n in ("lmbx", "lmby", "lmbz")]
+    # planes 0 and NY-1 are the walls, where the velocity and so the Lamb
+    # vector vanish: each component is measured against its largest value
+    # over the tested planes
+    worst = 0.0
+    for c in range(3):
+        a = np.stack([got[c][:, :, j] for j in planes])
+        b = np.stack([want[q][c] for q in range(len(planes))])
+        worst = max(worst, float(np.abs(a - b).max() / np.abs(b).max()))
+    print(f"Retau-550 case size: Lamb vector vs numpy on planes {planes}: max rel err {worst:.2e}")
+    assert worst < 1e-12
+    lamb = {n: g.get(n) for n in ("lmbx", "lmby", "lmbz")}
+    g.time_Integration(2)
+    for n in ("vely", "vory"):
+        assert np.isfinite(g.get(n)).all()
+    g.close()  # about 100 GB on the device per solver at this size
+    m = gpu_solver(p, precision="mixed")
+    m.init_fields(u, v, w)
+    for n, b in lamb.items():
+        d = float(np.linalg.norm((m.get(n) - b).ravel()) / np.linalg.norm(b.ravel()))
+        print(f"Retau-550 case size, mixed vs FP64 {n} relative L2: {d:.1e}")
+        assert d < 1e-6
+    m.time_Integration(2)
+    for n in ("vely", "vory"):
+        assert np.isfinite(m.get(n)).all()
+    m.close()
