@@ -184,10 +184,8 @@ struct owt_handle {
       throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must be of the form 2^a 3^b 5^c");
     if (NX2 > 1024 || NZ2 > 1024)
       throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 must not exceed 1024 (one thread per point of a line)");
-    px.L = NX2; px.nst = (int)rx.size();
-    for (size_t q = 0; q < rx.size(); ++q) px.R[q] = rx[q];
-    pz.L = NZ2; pz.nst = (int)rz.size();
-    for (size_t q = 0; q < rz.size(); ++q) pz.R[q] = rz[q];
+    if (!make_fft_plan(NX2, rx.data(), (int)rx.size(), px) || !make_fft_plan(NZ2, rz.data(), (int)rz.size(), pz))
+      throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 need at most 8 FFT stages");
     ck(cudaSetDevice(p.device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");

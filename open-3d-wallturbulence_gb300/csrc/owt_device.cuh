@@ -42,11 +42,43 @@ template <> __device__ __forceinline__ float2 from_d<float>(double2 a) { return 
 // exp(-2 pi i m / L); the backward transform (sign +1) uses its conjugate.
 // Unnormalised in both directions, like FFTW.
 // ---------------------------------------------------------------------------
+// A plan holds, per stage, the sizes the stage loop would otherwise divide out
+// (nr = L/R butterflies, ns points combined before it, twiddle stride
+// step = L/(ns R)) and multipliers ceil(2^32/d) for exact division by nr and
+// ns with a multiply-high (exact for n d < 2^32; 0 marks d = 1).  Lines of at
+// most 1024 points have at most 6 stages.
+constexpr int kFftMaxStages = 8;
 struct FftPlan {
   int L;
   int nst;
-  int R[12];
+  int8_t R[kFftMaxStages];
+  uint16_t nr[kFftMaxStages], ns[kFftMaxStages], step[kFftMaxStages];
+  uint32_t mnr[kFftMaxStages], mns[kFftMaxStages];
 };
+
+// quotient n / d with the plan's multiplier m for d (m = 0: d = 1)
+__device__ __forceinline__ int fft_div(int n, uint32_t m) { return m ? (int)__umulhi((unsigned)n, m) : n; }
+
+inline uint32_t fft_magic(int d) { return d > 1 ? (uint32_t)((((uint64_t)1 << 32) + (uint64_t)d - 1) / (uint64_t)d) : 0u; }
+// The plan for length L with the given stage radices (false if too many).
+inline bool make_fft_plan(int L, const int *radices, int nst, FftPlan &p) {
+  if (nst < 1 || nst > kFftMaxStages) return false;
+  p = FftPlan{};
+  p.L = L;
+  p.nst = nst;
+  int ns = 1;
+  for (int s = 0; s < nst; ++s) {
+    const int R = radices[s];
+    p.R[s] = (int8_t)R;
+    p.nr[s] = (uint16_t)(L / R);
+    p.ns[s] = (uint16_t)ns;
+    p.step[s] = (uint16_t)(L / (ns * R));
+    p.mnr[s] = fft_magic(L / R);
+    p.mns[s] = fft_magic(ns);
+    ns *= R;
+  }
+  return ns == L;
+}
 
 template <typename T, bool BACKWARD>
 __device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx) {
@@ -120,19 +152,16 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
 template <typename T, bool BACKWARD, bool R5>
 __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, const FftPlan &p,
                              const cpx<T> *__restrict__ tw) {
-  const int L = p.L;
   const int tid = threadIdx.x, nt = blockDim.x;
-  int ns = 1;
   for (int s = 0; s < p.nst; ++s) {
-    const int R = p.R[s];
-    const int nr = L / R;
-    const int step = L / (ns * R);
-    const int per = nt / nr;  // lines per pass
+    const int R = p.R[s], nr = p.nr[s], ns = p.ns[s], step = p.step[s];
+    const uint32_t mnr = p.mnr[s], mns = p.mns[s];
+    const int per = fft_div(nt, mnr);  // lines per pass
     if (per > 0) {
       if (tid < per * nr) {
-        const int j = tid % nr, lo = tid / nr;
-        const int k = j % ns;
-        const int base = (j - k) * R + k;
+        const int lo = fft_div(tid, mnr), j = tid - lo * nr;
+        const int q = fft_div(j, mns), k = j - q * ns;
+        const int base = q * ns * R + k;
         const bool twid = k != 0;
         cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1, w4 = w1;
         if (twid) {
@@ -146,8 +175,8 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
       }
     } else {
       for (int idx = tid; idx < nlines * nr; idx += nt) {
-        const int line = idx / nr, j = idx - line * nr;
-        const int k = j % ns;
+        const int line = fft_div(idx, mnr), j = idx - line * nr;
+        const int k = j - fft_div(j, mns) * ns;
         const bool twid = k != 0;
         cpx<T> w1 = mk<T>((T)1, (T)0), w2 = w1, w3 = w1, w4 = w1;
         if (twid) {
@@ -162,7 +191,6 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
     }
     __syncthreads();
     cpx<T> *tmp = a; a = b; b = tmp;
-    ns *= R;
   }
   return a;
 }

@@ -418,7 +418,7 @@ bool fft_radices(int L, std::vector<int> &r) {
   while (m % 2 == 0) { r.push_back(2); m /= 2; }
   while (m % 3 == 0) { r.push_back(3); m /= 3; }
   while (m % 5 == 0) { r.push_back(5); m /= 5; }
-  return m == 1 && r.size() <= 12;
+  return m == 1 && r.size() <= 8;
 }
 
 }  // namespace owt

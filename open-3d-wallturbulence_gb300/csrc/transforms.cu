@@ -31,8 +31,11 @@ namespace owt {
 template <typename T> struct XCfg;
 // TX lines per z block, P (y, z) lines per x block (3P FFT lines).  Blocks
 // have as many threads as the line length (NZ2 or NX2, at most 1024).
-template <> struct XCfg<double> { static constexpr int TX = 6; static constexpr int P = 4; };
-template <> struct XCfg<float> { static constexpr int TX = 12; static constexpr int P = 4; };
+// XREG caps the x-pass registers: 56 keeps two 576-thread FP32 blocks (whose
+// shared memory allows two) resident per SM; 64 is the bound of a 1024-thread
+// block.
+template <> struct XCfg<double> { static constexpr int TX = 6; static constexpr int P = 4; static constexpr int XREG = 64; };
+template <> struct XCfg<float> { static constexpr int TX = 12; static constexpr int P = 4; static constexpr int XREG = 56; };
 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(1024) k_zback(const __grid_constant__ XformArg
   zback_body<T, R5>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 template <typename T, int P, bool R5>
-__global__ void __launch_bounds__(1024) k_xlamb(const __grid_constant__ XformArgs a) {
+__global__ void __maxnreg__(XCfg<T>::XREG) k_xlamb(const __grid_constant__ XformArgs a) {
   xlamb_body<T, P, R5>(a, blockIdx.x);
 }
 template <typename T, bool R5>
@@ -278,7 +281,7 @@ __global__ void __launch_bounds__(1024) k_zback_batch(const __grid_constant__ Ba
   zback_body<T, R5>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
 }
 template <typename T, int P, bool R5>
-__global__ void __launch_bounds__(1024) k_xlamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+__global__ void __maxnreg__(XCfg<T>::XREG) k_xlamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
   const int c = batch_channel(t.start, t.n, blockIdx.x);
   xlamb_body<T, P, R5>(t.a[c], blockIdx.x - t.start[c]);
 }
