@@ -127,16 +127,17 @@ def test_batch_step_matches_individual_steps(gpu_lib):
 
 def test_batch_of_66_mixed_channels_matches_individual_steps(gpu_lib):
     """More channels than one launch table holds (64), FP64 and mixed-precision
-    channels, sixth-order channels (full-band solve), uneven sizes and one
-    channel with wall blowing/suction: every channel's bits equal stepping it
-    alone, and creating the batch (which times the mode-kernel variants on the
-    live state) leaves every channel's state untouched."""
+    channels, sixth-order channels (full-band solve), uneven sizes including
+    lines with a radix-5 stage, and one channel with wall blowing/suction:
+    every channel's bits equal stepping it alone, and creating the batch
+    (which times the mode-kernel variants on the live state) leaves every
+    channel's state untouched."""
     from owt.adjoint import seeded_wall_field
     from owt.batch import Batch
     from owt.ic import seeded_velocity
     from owt.params import CaseParams
     from owt.solver import GpuSolver
-    sizes = [(16, 33, 16), (16, 17, 24), (24, 33, 16), (32, 25, 16)]
+    sizes = [(16, 33, 16), (16, 17, 24), (24, 33, 16), (20, 25, 40)]  # the last: radix-5 lines
     ps, precs = [], []
     for q in range(66):
         nx, ny, nz = sizes[q % 4]
