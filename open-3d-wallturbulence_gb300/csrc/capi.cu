@@ -82,7 +82,8 @@ struct owt_handle {
   int precision = 0;
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;                    // the mean-mode branch of a step
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;    // the mean mode beside the mode kernel
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;  // the mean-flow terms beside the transforms
   std::vector<void *> owned;
   int64_t steps = 0;
   int64_t launches = 0;
@@ -104,6 +105,7 @@ struct owt_handle {
   double2 *u = nullptr, *w = nullptr, *ox = nullptr, *oz = nullptr, *lx = nullptr, *ly = nullptr, *lz = nullptr;
   double2 *U_ring = nullptr, *W_ring = nullptr, *lxm_ring = nullptr, *lzm_ring = nullptr;
   double *fx_ring = nullptr, *fz_ring = nullptr;
+  double2 *lm = nullptr;  // mixed precision: FP64 mean-flow terms of the Lamb vector [3][NY][M]
   long long *d_step = nullptr;
   int *d_err = nullptr;
   // factors and tables
@@ -136,8 +138,8 @@ struct owt_handle {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     for (void *q : owned) cudaFree(q);
-    if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
+      if (e) cudaEventDestroy(e);
     if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
@@ -191,6 +193,8 @@ struct owt_handle {
     ck(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_fork2, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_join2, cudaEventDisableTiming), "cudaEventCreate");
 
     // grid, metric, stencils, band templates (host, FP64)
     grid = make_grid(NY, p.alpha_mesh);
@@ -340,6 +344,7 @@ struct owt_handle {
     q_ring = dalloc<double2>(3 * fs, owned);
     for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &sv, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
       *f = dalloc<double2>(fs, owned);
+    lm = dalloc<double2>(3 * fs, owned);
     yv = dalloc<double2>((size_t)bv.n * M, owned);
     yg = dalloc<double2>((size_t)bg.n * M, owned);
     U_ring = dalloc<double2>(3 * (size_t)NY, owned);
@@ -398,6 +403,7 @@ struct owt_handle {
     a.fs = fs;
     a.step = d_step;
     a.mean_split = precision == OWT_PREC_MIXED ? 1 : 0;
+    for (int f = 0; f < 3; ++f) a.lm[f] = lm + (size_t)f * fs;
     a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
     a.zbuf = zbuf; a.lbuf = lbuf;
     a.px = px; a.pz = pz;
@@ -431,7 +437,22 @@ struct owt_handle {
     stage_modes();
     ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
     launch_advance(d_step, st);
-    const int nx = launch_lamb(xform_args(), precision, st);
+    const XformArgs xa = xform_args();
+    int nx = 3;
+    if (xa.mean_split) {
+      // the FP64 mean-flow terms beside the FP32 z backward and x pass
+      ck(cudaEventRecord(ev_fork2, st), "fork");
+      ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
+      launch_lamb_part(xa, precision, 3, st2);
+      ck(cudaEventRecord(ev_join2, st2), "join");
+      launch_lamb_part(xa, precision, 0, st);
+      launch_lamb_part(xa, precision, 1, st);
+      ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
+      launch_lamb_part(xa, precision, 2, st);
+      nx = 4;
+    } else {
+      nx = launch_lamb(xa, precision, st);
+    }
     launch_nl(nl_args(true), st);
     launches += 4 + nx;
   }
@@ -980,7 +1001,8 @@ static std::vector<TablePtr<A>> make_tables(const std::vector<A> &args, const st
 struct owt_batch {
   std::vector<owt_handle *> hs;
   cudaStream_t st = nullptr, st2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;    // the mean mode beside the mode kernel
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;  // the mean-flow terms beside the transforms
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int *work = nullptr;        // counter pairs of the persistent mode launches
@@ -1009,8 +1031,8 @@ struct owt_batch {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (work) cudaFree(work);
-    if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
+      if (e) cudaEventDestroy(e);
     if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
@@ -1119,9 +1141,22 @@ struct owt_batch {
       launch_advance_batch(c, st);
       ++step_launches;
     }
-    for (auto &l : lamb) {
-      launch_lamb_batch(*l.t, l.precision, l.part, st);
-      ++step_launches;
+    // the mean-flow terms of the mixed-precision channels beside the z
+    // backward and x pass; the z forward adds them
+    bool split = false;
+    for (auto &l : lamb) split = split || l.part == 3;
+    if (split) {
+      ck(cudaEventRecord(ev_fork2, st), "fork");
+      ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
+    }
+    for (int part : {3, 0, 1, 2}) {
+      if (part == 2 && split) ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
+      for (auto &l : lamb)
+        if (l.part == part) {
+          launch_lamb_batch(*l.t, l.precision, l.part, part == 3 ? st2 : st);
+          ++step_launches;
+        }
+      if (part == 3 && split) ck(cudaEventRecord(ev_join2, st2), "join");
     }
     for (auto &t : nl) {
       launch_nl_batch(*t, st);
@@ -1409,6 +1444,8 @@ int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
     ck(cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_fork2, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming), "event");
     const size_t n_mode_tables = (b->by_size(true).size() + kBatchChannels - 1) / kBatchChannels +
                                  (b->by_size(false).size() + kBatchChannels - 1) / kBatchChannels;
     ck(cudaMalloc(&b->work, 2 * n_mode_tables * sizeof(int)), "work counters");

@@ -120,6 +120,7 @@ struct XformArgs {
   // mixed precision: transform only the fluctuations (mode (0,0) left out)
   // and add the mean-flow interaction terms in FP64 in the last kernel
   int mean_split;
+  double2 *lm[3];  // mixed precision: the mean-flow terms [NY][M] each, added by the z forward
   double2 *out[3];
   void *zbuf;  // [6][NY][NZ2][NXH] complex<T>
   void *lbuf;  // [3][NY][NZ2][NXH] complex<T>
@@ -154,8 +155,10 @@ void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaS
 void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,
                   cudaStream_t st);
 
-// Lamb vector: z-backward (6 fields) -> x pass with products -> z-forward (3).
-// precision 0: FP64, 1: FP32 transforms and products.  Returns launches issued.
+// Lamb vector: z-backward (6 fields) -> x pass with products -> z-forward (3),
+// in mixed precision with the FP64 mean-flow terms (part 3) before the z
+// forward.  precision 0: FP64, 1: FP32 transforms and products.  Returns
+// launches issued.
 int launch_lamb(const XformArgs &a, int precision, cudaStream_t st);
 cudaError_t lamb_prepare(const XformDims &d);
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st);

@@ -168,21 +168,32 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
   __syncthreads();
   const cpx<T> *r = fft_lines<T, false, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
+  // mixed precision: plus the FP64 mean-flow terms k_mean_lamb wrote
+  const double2 *lm = a.mean_split ? a.lm[f] + (size_t)j * d.NZ * d.NXH : nullptr;
   const double sc = a.inv_nz2;
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
     const int kz = idx / TX, c = idx - kz * TX;
     if (i0 + c < d.NXH) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
       const double2 v = to_d(r[c * ls + slot]);
-      dst[(size_t)kz * d.NXH + i0 + c] = make_double2(v.x * sc, v.y * sc);
+      const size_t at = (size_t)kz * d.NXH + i0 + c;
+      double2 o = make_double2(v.x * sc, v.y * sc);
+      if (lm) {
+        const double2 l = lm[at];
+        o.x += l.x;
+        o.y += l.y;
+      }
+      dst[at] = o;
     }
   }
 }
 
-// Mixed precision: add, in FP64, the interaction of the mean flow with the
-// fluctuations that the FP32 transforms left out (mode (0, 0) is zeroed in
-// k_zback): lambda += Ubar x om + u x Obar at every mode and y, Ubar x Obar
-// at (0, 0), nothing on the Nyquist row (it never reaches physical space).
+// Mixed precision: the interaction of the mean flow with the fluctuations
+// that the FP32 transforms leave out (mode (0, 0) is zeroed in k_zback), in
+// FP64, written to lm for the z forward to add: Ubar x om + u x Obar at every
+// mode and y, Ubar x Obar at (0, 0), zero on the Nyquist row (it never reaches
+// physical space).  It reads only the step's fields, so it runs beside the z
+// backward and the x pass.
 // Ubar, Obar are the real parts of the (0, 0) modes of row j; the kx = 0
 // column enters through its Hermitian part, as the real-part extraction of
 // the x transform makes it enter the physical product.  Grid: (modes / 256,
@@ -193,9 +204,12 @@ __device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx,
   const int m = bx * 256 + threadIdx.x;
   if (m >= M) return;
   const int kz = m / d.NXH, kx = m - kz * d.NXH;
-  if (kz == d.NZH) return;
-  const int hd = ring_head(*a.step);
   const size_t row = (size_t)j * M, e = row + m;
+  if (kz == d.NZH) {
+    for (int f = 0; f < 3; ++f) a.lm[f][e] = make_double2(0.0, 0.0);
+    return;
+  }
+  const int hd = ring_head(*a.step);
   const double2 *base[6];
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
@@ -222,13 +236,11 @@ __device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx,
     // drops their terms: Ubar x om + u x Obar with Ubar = (U, 0, W), Obar =
     // (Ox, 0, Oz).
     if (m != 0 && Ub[1] == 0.0 && Ob[1] == 0.0) {
-      double2 *o0 = a.out[0] + e, *o1 = a.out[1] + e, *o2 = a.out[2] + e;
-      const double2 l0 = *o0, l1 = *o1, l2 = *o2;
       // x: -W oy + v Oz ; y: W ox - U oz + w Ox - u Oz ; z: U oy - v Ox
-      *o0 = make_double2(l0.x - Ub[2] * F[4].x + F[1].x * Ob[2], l0.y - Ub[2] * F[4].y + F[1].y * Ob[2]);
-      *o1 = make_double2(l1.x + Ub[2] * F[3].x - Ub[0] * F[5].x + F[2].x * Ob[0] - F[0].x * Ob[2],
-                         l1.y + Ub[2] * F[3].y - Ub[0] * F[5].y + F[2].y * Ob[0] - F[0].y * Ob[2]);
-      *o2 = make_double2(l2.x + Ub[0] * F[4].x - F[1].x * Ob[0], l2.y + Ub[0] * F[4].y - F[1].y * Ob[0]);
+      a.lm[0][e] = make_double2(F[1].x * Ob[2] - Ub[2] * F[4].x, F[1].y * Ob[2] - Ub[2] * F[4].y);
+      a.lm[1][e] = make_double2(Ub[2] * F[3].x - Ub[0] * F[5].x + F[2].x * Ob[0] - F[0].x * Ob[2],
+                                Ub[2] * F[3].y - Ub[0] * F[5].y + F[2].y * Ob[0] - F[0].y * Ob[2]);
+      a.lm[2][e] = make_double2(Ub[0] * F[4].x - F[1].x * Ob[0], Ub[0] * F[4].y - F[1].y * Ob[0]);
       return;
     }
 #pragma unroll
@@ -243,9 +255,7 @@ __device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx,
         l = make_double2(Ub[f1] * o2.x - Ub[f2] * o1.x + u1.x * Ob[f2] - u2.x * Ob[f1],
                          Ub[f1] * o2.y - Ub[f2] * o1.y + u1.y * Ob[f2] - u2.y * Ob[f1]);
       }
-      double2 *o = a.out[f] + e;
-      const double2 v = *o;
-      *o = make_double2(v.x + l.x, v.y + l.y);
+      a.lm[f][e] = l;
     }
   }
 }
@@ -363,9 +373,12 @@ static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   }
 }
 
+// On one stream: the mean-flow terms (mixed precision) first, as the z
+// forward adds them.
 template <typename T>
 static int lamb_t(const XformArgs &a, cudaStream_t st) {
-  for (int part = 0; part < 4; ++part) lamb_part_t<T>(a, part, st);
+  if (a.mean_split) lamb_part_t<T>(a, 3, st);
+  for (int part = 0; part < 3; ++part) lamb_part_t<T>(a, part, st);
   return a.mean_split ? 4 : 3;
 }
 
