@@ -418,7 +418,7 @@ struct owt_handle {
     a.lx = lx; a.ly = ly; a.lz = lz;
     a.hv_ring = hv_ring; a.hg_ring = hg_ring;
     a.ab1 = b1.ab; a.piv1 = b1.piv; a.b1_col = b1_col; a.b1_val = b1_val;
-    a.bf = bf; a.yscr = yscr;
+    a.yscr = yscr;
     a.lx_mean = record_mean ? lxm_ring : nullptr;
     a.lz_mean = record_mean ? lzm_ring : nullptr;
     a.step = d_step;

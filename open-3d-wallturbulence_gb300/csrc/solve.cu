@@ -347,23 +347,24 @@ __device__ __forceinline__ void nl_body(const NLArgs &a, const int m) {
     const double2 x = a.lx[(size_t)j * M + m], z = a.lz[(size_t)j * M + m];
     return make_double2(-kx * x.y - kz * z.y, kx * x.x + kz * z.x);
   };
-  for (int j = 0; j < NY; ++j) {
+  // The solve asks for each right-hand side once, in increasing row order:
+  // row p's B1 (i kx lx + i kz lz) is formed there, and Hg of row p with it.
+  auto rhs = [&](int p) -> double2 {
     double2 acc = make_double2(0.0, 0.0);
 #pragma unroll
     for (int e = 0; e < 5; ++e) {
-      const double b = a.b1_val[j * 5 + e];
+      const double b = a.b1_val[p * 5 + e];
       if (b != 0.0) {
-        const double2 f = fval(a.b1_col[j * 5 + e]);
+        const double2 f = fval(a.b1_col[p * 5 + e]);
         acc.x += b * f.x;
         acc.y += b * f.y;
       }
     }
-    const size_t at = (size_t)j * M + m;
-    a.bf[at] = acc;
+    const size_t at = (size_t)p * M + m;
     const double2 x = a.lx[at], z = a.lz[at];
     hg[at] = make_double2(-kz * x.y + kx * z.y, kz * x.x - kx * z.x);
-  }
-  auto rhs = [&](int p) -> double2 { return a.bf[(size_t)p * M + m]; };
+    return acc;
+  };
   auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
   auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
   auto out = [&](int c, double2 d) {

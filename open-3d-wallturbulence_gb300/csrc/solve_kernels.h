@@ -74,7 +74,7 @@ struct NLArgs {
   double2 *hv_ring, *hg_ring;
   const double *ab1; const uint8_t *piv1;
   const int *b1_col; const double *b1_val;
-  double2 *bf, *yscr;
+  double2 *yscr;               // forward-sweep scratch [NY][M]
   double2 *lx_mean, *lz_mean;  // rings [3][NY], or null
   const long long *step;
 };
