@@ -117,8 +117,9 @@ struct XformArgs {
   int ring_mask;
   size_t fs;
   const long long *step;
-  // mixed precision: transform only the fluctuations (mode (0,0) left out)
-  // and add the mean-flow interaction terms in FP64 in the last kernel
+  // mixed precision (FP32 transforms only): transform only the fluctuations
+  // (mode (0,0) left out); k_mean_lamb writes the FP64 mean-flow interaction
+  // terms to lm and the z forward adds them
   int mean_split;
   double2 *lm[3];  // mixed precision: the mean-flow terms [NY][M] each, added by the z forward
   double2 *out[3];

@@ -168,8 +168,10 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
   __syncthreads();
   const cpx<T> *r = fft_lines<T, false, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
-  // mixed precision: plus the FP64 mean-flow terms k_mean_lamb wrote
-  const double2 *lm = a.mean_split ? a.lm[f] + (size_t)j * d.NZ * d.NXH : nullptr;
+  // mixed precision (FP32 transforms): plus the FP64 mean-flow terms
+  // k_mean_lamb wrote; the FP64 instances carry no such epilogue
+  constexpr bool kSplit = sizeof(T) == sizeof(float);
+  const double2 *lm = (kSplit && a.mean_split) ? a.lm[f] + (size_t)j * d.NZ * d.NXH : nullptr;
   const double sc = a.inv_nz2;
   for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
     const int kz = idx / TX, c = idx - kz * TX;
@@ -178,7 +180,7 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
       const double2 v = to_d(r[c * ls + slot]);
       const size_t at = (size_t)kz * d.NXH + i0 + c;
       double2 o = make_double2(v.x * sc, v.y * sc);
-      if (lm) {
+      if (kSplit && lm) {
         const double2 l = lm[at];
         o.x += l.x;
         o.y += l.y;
