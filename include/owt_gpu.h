@@ -117,6 +117,15 @@ const char *owt_last_error(const owt_handle *h);
  * histories.  velx/vely/velz: [z][x][y] complex128. */
 int owt_init_fields(owt_handle *h, const double *velx, const double *vely, const double *velz);
 
+/* init_fields with a seeded velocity generated on the device (no counterpart
+ * in the reference, whose initial conditions are laminar, laminar + TS wave,
+ * or a restart): laminar Poiseuille flow 1.5 (1 - y^2) plus a divergence-free
+ * perturbation with complex Gaussian Chebyshev amplitudes (degree 5) under a
+ * k^-2 spectrum, v, dv/dy and omega_y zero at the walls, scaled to RMS `rms`
+ * (Parseval, trapezoidal in y).  Random numbers: Philox4x32-10 keyed by the
+ * seed and counted per mode, so a seed gives the same field on every call. */
+int owt_init_seeded(owt_handle *h, uint64_t seed, double rms);
+
 /* time_Integration (src/solver.cpp:541-627), nsteps times. Asynchronous on
  * the handle's stream; errors found on the device surface at the next
  * synchronizing call. */

@@ -106,6 +106,8 @@ struct owt_handle {
   double2 *U_ring = nullptr, *W_ring = nullptr, *lxm_ring = nullptr, *lzm_ring = nullptr;
   double *fx_ring = nullptr, *fz_ring = nullptr;
   double2 *lm = nullptr;  // mixed precision: FP64 mean-flow terms of the Lamb vector [3][NY][M]
+  double *ygrid = nullptr, *wy = nullptr;  // y and its trapezoidal weights (summing to 1)
+  double *ic_partial = nullptr;            // seeded initial condition: RMS partial sums
   long long *d_step = nullptr;
   int *d_err = nullptr;
   // factors and tables
@@ -345,6 +347,20 @@ struct owt_handle {
     for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &sv, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
       *f = dalloc<double2>(fs, owned);
     lm = dalloc<double2>(3 * fs, owned);
+    {
+      std::vector<double> wyh(NY, 0.0);
+      double tot = 0.0;
+      for (int j = 0; j + 1 < NY; ++j) {
+        const double h = grid.y[j + 1] - grid.y[j];
+        wyh[j] += 0.5 * h;
+        wyh[j + 1] += 0.5 * h;
+      }
+      for (double x : wyh) tot += x;
+      for (double &x : wyh) x /= tot;
+      ygrid = upload(grid.y, owned, st);
+      wy = upload(wyh, owned, st);
+      ic_partial = dalloc<double>(ic_partial_values(), owned);
+    }
     yv = dalloc<double2>((size_t)bv.n * M, owned);
     yg = dalloc<double2>((size_t)bg.n * M, owned);
     U_ring = dalloc<double2>(3 * (size_t)NY, owned);
@@ -660,14 +676,38 @@ struct owt_handle {
     ++launches;
   }
 
-  void init_fields(const double *hu, const double *hv, const double *hw) {
+  void init_prologue() {
     steps = 0;
     drop_graph();
     ck(cudaMemsetAsync(d_step, 0, sizeof(long long), st), "memset");
     ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "memset");
+  }
+  void init_fields(const double *hu, const double *hv, const double *hw) {
+    init_prologue();
     to_device(hu, u);
     to_device(hv, ring_level(v_ring, 0));
     to_device(hw, w);
+    init_from_velocity();
+  }
+  // The seeded laminar + random divergence-free state, generated on the
+  // device (seeded_ic.cu); the Chebyshev coefficients live in the mean-flow
+  // buffer and omega_y in tmpC until the velocity is complete.
+  void init_seeded(uint64_t seed, double rms) {
+    init_prologue();
+    SeedArgs a{};
+    a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.degree = 5;
+    a.seed = seed;
+    a.kmin = std::min(p.dkx, p.dkz);
+    a.kx = kx; a.kz = kz; a.y = ygrid; a.c11 = c11; a.wy = wy;
+    a.coef = lm;  // 3 NY M >= 12 M values
+    double2 *v0 = ring_level(v_ring, 0);
+    launches += launch_ic_fields(a, v0, tmpC, st);
+    dapply(1, v0, tmpA);
+    launches += launch_ic_velocity(a, tmpA, tmpC, u, v0, w, ic_partial, rms, st);
+    check_launch("seeded initial condition");
+    init_from_velocity();
+  }
+  void init_from_velocity() {
     get_vor_from_vel();  // also leaves D1 u, D1 w in tmpA, tmpB
     launch_friction(tmpA, tmpB, c11, NY, M, p.nu, Ly, fx_ring, fz_ring, d_step, 0, d_err, st);
     ++launches;
@@ -1276,6 +1316,15 @@ int owt_init_fields(owt_handle *h, const double *velx, const double *vely, const
     if (!velx || !vely || !velz) throw OwtError(OWT_ERR_INVALID, "null field");
     ++h->state_version;
     h->init_fields(velx, vely, velz);
+    h->sync_and_check();
+  });
+}
+
+int owt_init_seeded(owt_handle *h, uint64_t seed, double rms) {
+  return guard(h, [&] {
+    if (!(rms >= 0.0)) throw OwtError(OWT_ERR_INVALID, "rms must be non-negative");
+    ++h->state_version;
+    h->init_seeded(seed, rms);
     h->sync_and_check();
   });
 }

@@ -166,6 +166,21 @@ void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t 
 size_t lamb_zbuf_bytes(const XformDims &d, int precision);
 size_t lamb_lbuf_bytes(const XformDims &d, int precision);
 
+// Seeded initial condition (seeded_ic.cu): Chebyshev coefficients per mode
+// from a counter-based generator, v and omega_y, then u, w and the RMS scaling.
+struct SeedArgs {
+  int NY, NZ, NXH, NZH, M, degree;
+  uint64_t seed;
+  double kmin;
+  const double *kx, *kz, *y, *c11, *wy;  // wy: trapezoidal weights in y, summing to 1
+  double2 *coef;                          // [M][2][degree + 1]
+};
+size_t ic_coef_values(int M, int degree);
+size_t ic_partial_values();
+int launch_ic_fields(const SeedArgs &a, double2 *v, double2 *g, cudaStream_t st);
+int launch_ic_velocity(const SeedArgs &a, const double2 *d1v_raw, const double2 *g, double2 *u, double2 *v,
+                       double2 *w, double *partial, double rms, cudaStream_t st);
+
 // Batch tables travel as kernel parameters, which are limited to 32764 bytes.
 static_assert(sizeof(BatchTable<ModeArgs>) <= 32764, "mode-kernel batch table exceeds the kernel parameter limit");
 static_assert(sizeof(BatchTable<XformArgs>) <= 32764, "transform batch table exceeds the kernel parameter limit");

@@ -60,6 +60,11 @@ class GpuSolver:
         u, v, w = self._c(velx), self._c(vely), self._c(velz)
         self._chk(self.L.owt_init_fields(self.h, *[_L.dptr(x.view(np.float64)) for x in (u, v, w)]))
 
+    def init_seeded(self, seed=0, rms=0.1):
+        """init_fields with the laminar + seeded random divergence-free
+        velocity generated on the device (owt_init_seeded)."""
+        self._chk(self.L.owt_init_seeded(self.h, int(seed), float(rms)))
+
     def time_Integration(self, nsteps=1):
         self._chk(self.L.owt_time_integration(self.h, int(nsteps)))
 
