@@ -247,6 +247,13 @@ const char *owt_tuning_report(const owt_handle *h);
  * pattern check, fields and tables, mode-kernel autotune), as text. */
 const char *owt_setup_report(const owt_handle *h);
 
+/* Testing aid: factor U random band systems (kl/ku as the library's: 15/13,
+ * 6/6, 2/2) of n columns with both factorization kernels (thread per system;
+ * warp per system, used when a channel has few modes), count the entries of
+ * the factors, pivots and row scales that differ bitwise, and time each. */
+int owt_band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, int64_t *mismatches, float *ms_thread,
+                             float *ms_warp);
+
 /* Measurement aid, no counterpart in the reference: enqueue one stage of the
  * step on the handle's stream without advancing the step counter, so a caller
  * can time it with CUDA events on that stream.  The stage overwrites the

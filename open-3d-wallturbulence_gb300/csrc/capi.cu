@@ -1320,6 +1320,22 @@ int owt_init_fields(owt_handle *h, const double *velx, const double *vely, const
   });
 }
 
+int owt_band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, int64_t *mismatches, float *ms_thread,
+                             float *ms_warp) {
+  if (!mismatches || !ms_thread || !ms_warp || n < 1 || U < 1 || !band_supported(kl, ku)) {
+    g_create_error = "owt_band_factor_selftest: bad arguments";
+    return OWT_ERR_INVALID;
+  }
+  long long bad = 0;
+  if (band_factor_selftest(kl, ku, n, U, seed, &bad, ms_thread, ms_warp) != 0) {
+    g_create_error = "owt_band_factor_selftest: CUDA error";
+    cudaGetLastError();
+    return OWT_ERR_CUDA;
+  }
+  *mismatches = bad;
+  return OWT_OK;
+}
+
 int owt_init_seeded(owt_handle *h, uint64_t seed, double rms) {
   return guard(h, [&] {
     if (!(rms >= 0.0)) throw OwtError(OWT_ERR_INVALID, "rms must be non-negative");

@@ -13,6 +13,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
+#include <random>
+#include <vector>
+
 #include "owt_device.cuh"
 #include "solve_kernels.h"
 #include "modes_kernel.cuh"
@@ -43,7 +47,7 @@ __global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv
       double v = 0.0;
       if (b >= KL) {
         const size_t at = (size_t)(b - KL) * n + c;
-        v = t0[at] + a1 * t1[at] + a2 * t2[at];
+        v = __fma_rn(a2, t2[at], __fma_rn(a1, t1[at], t0[at]));
       }
       AB(b, c) = v;
     }
@@ -84,22 +88,216 @@ __global__ void k_band_factor(double *__restrict__ ab, uint8_t *__restrict__ piv
     for (int c = j + 1; c <= ju; ++c) {
       const double t = AB(KV - (c - j), c);
       if (t != 0.0)
-        for (int i = 1; i <= km; ++i) AB(KV + i - (c - j), c) -= AB(KV + i, j) * t;
+        for (int i = 1; i <= km; ++i) {
+          double &x = AB(KV + i - (c - j), c);
+          x = __fma_rn(-AB(KV + i, j), t, x);
+        }
     }
   }
   for (int j = 0; j < n; ++j) AB(KV, j) = 1.0 / AB(KV, j);
 }
 
+// Warp-cooperative form of k_band_factor for systems with few modes (a
+// thread-per-mode LU is latency-bound when a channel has only hundreds of
+// modes): one warp per unique mode, the active columns [j, j + KV] of its band
+// in a shared-memory window (column c in slot c mod (KV + 1)); pivot search,
+// interchange, scaling and the rank-1 update spread over the lanes.  Every
+// element sees the same operations in the same order as in k_band_factor, so
+// the factors are bitwise the same.  Rows are equilibrated as they enter the
+// window: row p is first touched by the step of column p - KL, and its entries
+// span columns p - KL .. p + KU, all in the window then and still unmodified.
+template <int KL, int KU, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS)
+    k_band_factor_warp(double *__restrict__ ab, uint8_t *__restrict__ piv, int n, int U, const double *__restrict__ t0,
+                       const double *__restrict__ t1, const double *__restrict__ t2, const double *__restrict__ s1,
+                       const double *__restrict__ s2, double *__restrict__ rscale, int *__restrict__ info) {
+  constexpr int KV = KL + KU, NB = 2 * KL + KU + 1, WC = KV + 1;
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ double win[WARPS][WC * NB];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int u = blockIdx.x * WARPS + wq;
+  if (u >= U) return;  // the whole warp
+  double *w = win[wq];
+  const size_t sn = (size_t)n * U;
+  auto W = [&](int b, int c) -> double & { return w[(c % WC) * NB + b]; };
+  const double a1 = s1 ? s1[u] : 0.0, a2 = s2 ? s2[u] : 0.0;
+  auto load_col = [&](int c) {
+    for (int b = lane; b < NB; b += 32) {
+      double v = 0.0;
+      if (b >= KL) {
+        const size_t at = (size_t)(b - KL) * n + c;
+        v = __fma_rn(a2, t2[at], __fma_rn(a1, t1[at], t0[at]));
+      }
+      W(b, c) = v;
+    }
+  };
+  auto equilibrate = [&](int p) {  // row p holds A(p, c) at band row KV + p - c
+    const int c0 = max(0, p - KL), c1 = min(n - 1, p + KU);
+    double mx = 0.0;
+    for (int c = c0 + lane; c <= c1; c += 32) mx = fmax(mx, fabs(W(KV + p - c, c)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL, mx, o));
+    const double inv = mx > 0.0 ? 1.0 / mx : 1.0;
+    for (int c = c0 + lane; c <= c1; c += 32) W(KV + p - c, c) *= inv;
+    if (lane == 0) rscale[(size_t)p * U + u] = inv;
+  };
+  for (int c = 0; c <= min(n - 1, KV); ++c) load_col(c);
+  __syncwarp();
+  if (rscale)
+    for (int p = 0; p <= min(n - 1, KL); ++p) equilibrate(p);
+  __syncwarp();
+  int ju = 0;
+  for (int j = 0; j < n; ++j) {
+    const int km = min(KL, n - 1 - j);
+    // pivot: the first entry of maximal magnitude among rows j .. j + km
+    unsigned long long key = 0ull;
+    int jp = 0x7fffffff;
+    if (lane <= km) {
+      const double v = fabs(W(KV + lane, j));
+      key = v == v ? (unsigned long long)__double_as_longlong(v) : 0ull;  // non-negative: bits order as values
+      jp = lane;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(FULL, key, o);
+      const int oj = __shfl_xor_sync(FULL, jp, o);
+      if (ok > key || (ok == key && oj < jp)) {
+        key = ok;
+        jp = oj;
+      }
+    }
+    if (lane == 0) piv[(size_t)j * U + u] = (uint8_t)jp;
+    if (W(KV + jp, j) == 0.0) {
+      if (lane == 0) atomicMax(info, 1);
+    } else {
+      ju = max(ju, min(j + KU + jp, n - 1));
+      if (jp != 0)
+        for (int c = j + lane; c <= ju; c += 32) {
+          double &x = W(KV + jp - (c - j), c);
+          double &y = W(KV - (c - j), c);
+          const double t = x;
+          x = y;
+          y = t;
+        }
+      __syncwarp();
+      const double rp = 1.0 / W(KV, j);
+      for (int i = 1 + lane; i <= km; i += 32) W(KV + i, j) *= rp;
+      __syncwarp();
+      const int total = (ju - j) * km;
+      for (int q = lane; q < total; q += 32) {
+        const int cc = q / km, i = q - cc * km + 1, c = j + 1 + cc;
+        const double t = W(KV - (c - j), c);  // row j: not written in this step
+        if (t != 0.0) {
+          double &x = W(KV + i - (c - j), c);
+          x = __fma_rn(-W(KV + i, j), t, x);
+        }
+      }
+    }
+    __syncwarp();
+    // column j is final: out to the factors, the diagonal as its reciprocal
+    for (int b = lane; b < NB; b += 32) {
+      double v = W(b, j);
+      if (b == KV) v = 1.0 / v;
+      ab[(size_t)b * sn + (size_t)j * U + u] = v;
+    }
+    __syncwarp();
+    if (j + WC < n) load_col(j + WC);  // into column j's slot
+    __syncwarp();
+    if (rscale && j + 1 + KL < n) equilibrate(j + 1 + KL);
+    __syncwarp();
+  }
+}
+
+// kernel: 1 thread per mode, 2 warp per mode, 0 by the number of modes (the
+// warp form when the thread form would leave the GPU mostly idle)
+template <int KL, int KU>
+static void factor_t(int kernel, double *ab, uint8_t *piv, int n, int U, const double *t0, const double *t1,
+                     const double *t2, const double *s1, const double *s2, double *rscale, int *info,
+                     cudaStream_t st) {
+  if (kernel == 0) kernel = U < kBandFactorWarpBelow ? 2 : 1;
+  if (kernel == 2) {
+    constexpr int WARPS = 4;
+    k_band_factor_warp<KL, KU, WARPS><<<(U + WARPS - 1) / WARPS, 32 * WARPS, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1,
+                                                                                      s2, rscale, info);
+  } else {
+    const int bs = 64, gs = (U + bs - 1) / bs;
+    k_band_factor<KL, KU><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
+  }
+}
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0,
                         const double *t1, const double *t2, const double *s1, const double *s2, double *rscale,
-                        int *info, cudaStream_t st) {
-  const int bs = 64, gs = (U + bs - 1) / bs;
-  if (kl == 15 && ku == 13)
-    k_band_factor<15, 13><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
-  else if (kl == 6 && ku == 6)
-    k_band_factor<6, 6><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
-  else if (kl == 2 && ku == 2)
-    k_band_factor<2, 2><<<gs, bs, 0, st>>>(ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info);
+                        int *info, cudaStream_t st, int kernel) {
+  if (kl == 15 && ku == 13) factor_t<15, 13>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
+  else if (kl == 6 && ku == 6) factor_t<6, 6>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
+  else if (kl == 2 && ku == 2) factor_t<2, 2>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
+}
+
+// Both factorization kernels on the same random systems: bitwise comparison
+// of factors, pivots and row scales, and the time of each (testing aid).
+int band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, long long *mismatches, float *ms_thread,
+                         float *ms_warp) {
+  const int rows = kl + ku + 1, nb = 2 * kl + ku + 1;
+  std::mt19937_64 gen(seed);
+  std::normal_distribution<double> nd(0.0, 1.0);
+  std::vector<double> t[3], s[2];
+  for (auto &v : t) { v.resize((size_t)rows * n); for (double &x : v) x = nd(gen); }
+  for (auto &v : s) { v.resize(U); for (double &x : v) x = nd(gen); }
+  const size_t nab = (size_t)nb * n * U, np = (size_t)n * U;
+  double *d_t[3] = {}, *d_s[2] = {}, *ab[2] = {}, *rs[2] = {};
+  uint8_t *pv[2] = {};
+  int *info = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = cudaSuccess;
+  auto chk = [&](cudaError_t e) { if (err == cudaSuccess) err = e; };
+  for (int q = 0; q < 3; ++q) {
+    chk(cudaMalloc(&d_t[q], t[q].size() * sizeof(double)));
+    if (err == cudaSuccess) chk(cudaMemcpy(d_t[q], t[q].data(), t[q].size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  for (int q = 0; q < 2; ++q) {
+    chk(cudaMalloc(&d_s[q], (size_t)U * sizeof(double)));
+    if (err == cudaSuccess) chk(cudaMemcpy(d_s[q], s[q].data(), (size_t)U * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMalloc(&ab[q], nab * sizeof(double)));
+    chk(cudaMalloc(&rs[q], np * sizeof(double)));
+    chk(cudaMalloc(&pv[q], np));
+  }
+  chk(cudaMalloc(&info, sizeof(int)));
+  chk(cudaEventCreate(&e0));
+  chk(cudaEventCreate(&e1));
+  float ms[2] = {0.f, 0.f};
+  if (err == cudaSuccess) {
+    for (int q = 0; q < 2; ++q) {
+      launch_band_factor(kl, ku, ab[q], pv[q], n, U, d_t[0], d_t[1], d_t[2], d_s[0], d_s[1], rs[q], info, 0, q + 1);
+      chk(cudaEventRecord(e0, 0));
+      launch_band_factor(kl, ku, ab[q], pv[q], n, U, d_t[0], d_t[1], d_t[2], d_s[0], d_s[1], rs[q], info, 0, q + 1);
+      chk(cudaEventRecord(e1, 0));
+      chk(cudaEventSynchronize(e1));
+      chk(cudaGetLastError());
+      if (err == cudaSuccess) chk(cudaEventElapsedTime(&ms[q], e0, e1));
+    }
+  }
+  long long bad = 0;
+  if (err == cudaSuccess) {
+    std::vector<double> a(nab), b(nab), ra(np), rb(np);
+    std::vector<uint8_t> pa(np), pb(np);
+    chk(cudaMemcpy(a.data(), ab[0], nab * sizeof(double), cudaMemcpyDeviceToHost));
+    chk(cudaMemcpy(b.data(), ab[1], nab * sizeof(double), cudaMemcpyDeviceToHost));
+    chk(cudaMemcpy(ra.data(), rs[0], np * sizeof(double), cudaMemcpyDeviceToHost));
+    chk(cudaMemcpy(rb.data(), rs[1], np * sizeof(double), cudaMemcpyDeviceToHost));
+    chk(cudaMemcpy(pa.data(), pv[0], np, cudaMemcpyDeviceToHost));
+    chk(cudaMemcpy(pb.data(), pv[1], np, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < nab; ++q) bad += std::memcmp(&a[q], &b[q], sizeof(double)) != 0;
+    for (size_t q = 0; q < np; ++q) bad += (std::memcmp(&ra[q], &rb[q], sizeof(double)) != 0) + (pa[q] != pb[q]);
+  }
+  for (int q = 0; q < 3; ++q) cudaFree(d_t[q]);
+  for (int q = 0; q < 2; ++q) { cudaFree(d_s[q]); cudaFree(ab[q]); cudaFree(rs[q]); cudaFree(pv[q]); }
+  cudaFree(info);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (err != cudaSuccess) return -1;
+  *mismatches = bad;
+  *ms_thread = ms[0];
+  *ms_warp = ms[1];
+  return 0;
 }
 
 bool band_supported(int kl, int ku) {

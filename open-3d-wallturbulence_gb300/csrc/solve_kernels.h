@@ -131,9 +131,14 @@ struct XformArgs {
 };
 
 bool band_supported(int kl, int ku);
+int band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, long long *mismatches, float *ms_thread,
+                         float *ms_warp);
+// Band LU of U systems (dgbtf2 order, row equilibration when rscale is given).
+// kernel: 1 thread per system, 2 one warp per system, 0 chosen by U.
+constexpr int kBandFactorWarpBelow = 32768;
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0, const double *t1,
                         const double *t2, const double *s1, const double *s2, double *rscale, int *info,
-                        cudaStream_t st);
+                        cudaStream_t st, int kernel = 0);
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
 int modes_variant_count();
 const char *modes_variant_name(int v);

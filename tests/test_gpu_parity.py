@@ -481,3 +481,17 @@ def test_reference_retau550_case_size_lamb_vector_and_steps(gpu_lib):
     for n in ("vely", "vory"):
         assert np.isfinite(m.get(n)).all()
     m.close()
+
+
+@pytest.mark.parametrize("kl,ku,n,U", [(15, 13, 264, 600), (15, 13, 392, 1500), (6, 6, 196, 700), (2, 2, 97, 1),
+                                       (15, 13, 1028, 2048)])
+def test_warp_band_factorization_is_bitwise_the_thread_one(gpu_lib, kl, ku, n, U):
+    """The warp-per-system LU (channels with few modes) gives the same bits as
+    the thread-per-system LU: factors, pivots and row scales."""
+    import ctypes as C
+    from owt import lib as L
+    lib = L.load(gpu_lib)
+    bad, t1, t2 = C.c_int64(-1), C.c_float(0), C.c_float(0)
+    assert lib.owt_band_factor_selftest(kl, ku, n, U, 1234 + n, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK
+    print(f"kl={kl} ku={ku} n={n} U={U}: thread {t1.value:.3f} ms, warp {t2.value:.3f} ms")
+    assert bad.value == 0
