@@ -101,9 +101,10 @@ def _torch_reference(p, s, vb, vt, nsteps):
     return J.item(), vbt.grad.numpy(), vtt.grad.numpy()
 
 
-@pytest.mark.parametrize("nsteps,interval", [(6, 4), (5, 1), (4, 10)])
-def test_adjoint_matches_autodiff_reference(gpu_lib, port_lib, nsteps, interval):
-    p = _case()
+@pytest.mark.parametrize("nsteps,interval,size", [(6, 4, None), (5, 1, None), (4, 10, None), (4, 2, (20, 21, 40))])
+def test_adjoint_matches_autodiff_reference(gpu_lib, port_lib, nsteps, interval, size):
+    """The last case has lines with a radix-5 stage (3NX/2, 3NZ/2 = 30, 60)."""
+    p = _case() if size is None else _case(NX=size[0], NY=size[1], NZ=size[2])
     vb, vt = _walls(p)
     s = _solver(p)
     s.time_Integration(2)  # start from a state with distinct history levels
