@@ -80,6 +80,22 @@ inline bool make_fft_plan(int L, const int *radices, int nst, FftPlan &p) {
   return ns == L;
 }
 
+// Position of point i of a line in shared memory.  FP32 lines (8-byte
+// values, 16 per 128-byte wavefront) permute each aligned block of 16 by
+// i ^ 5 ((i >> 4) & 3): the stride-R stores of the first two radix-4 stages
+// then hit 16 different bank pairs per half-warp instead of 4, and runs of
+// consecutive points stay conflict-free.  A line occupies whole blocks
+// (line_stride).  FP64 lines are stored as they are.
+template <typename T>
+__device__ __forceinline__ int sw(int i) {
+  if (sizeof(T) == sizeof(float)) return i ^ (5 * ((i >> 4) & 3));
+  return i;
+}
+template <typename T>
+__host__ __device__ __forceinline__ int line_stride(int L) {
+  return (sizeof(T) == sizeof(float) ? (L + 15) / 16 * 16 : L) + 1;
+}
+
 template <typename T, bool BACKWARD>
 __device__ __forceinline__ cpx<T> twiddle(const cpx<T> *__restrict__ tw, int idx) {
   cpx<T> w = tw[idx];
@@ -91,27 +107,28 @@ template <typename T, bool BACKWARD, bool R5>
 __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R, int j, int nr, int ns, int base,
                                           cpx<T> w1, cpx<T> w2, cpx<T> w3, cpx<T> w4, bool twid) {
   if (R == 4) {
-    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr];
+    cpx<T> x0 = src[sw<T>(j)], x1 = src[sw<T>(j + nr)], x2 = src[sw<T>(j + 2 * nr)], x3 = src[sw<T>(j + 3 * nr)];
     if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); }
     const cpx<T> t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
     const cpx<T> d = csub(x1, x3);
     // t3 = d * (sign i): forward multiplies by -i, backward by +i
     const cpx<T> t3 = BACKWARD ? mk<T>(-d.y, d.x) : mk<T>(d.y, -d.x);
-    dst[base] = cadd(t0, t2);
-    dst[base + ns] = cadd(t1, t3);
-    dst[base + 2 * ns] = csub(t0, t2);
-    dst[base + 3 * ns] = csub(t1, t3);
+    dst[sw<T>(base)] = cadd(t0, t2);
+    dst[sw<T>(base + ns)] = cadd(t1, t3);
+    dst[sw<T>(base + 2 * ns)] = csub(t0, t2);
+    dst[sw<T>(base + 3 * ns)] = csub(t1, t3);
   } else if (R == 2) {
-    cpx<T> x0 = src[j], x1 = src[j + nr];
+    cpx<T> x0 = src[sw<T>(j)], x1 = src[sw<T>(j + nr)];
     if (twid) x1 = cmul(x1, w1);
-    dst[base] = cadd(x0, x1);
-    dst[base + ns] = csub(x0, x1);
+    dst[sw<T>(base)] = cadd(x0, x1);
+    dst[sw<T>(base + ns)] = csub(x0, x1);
   } else if (R5 && R == 5) {
     // DFT of length 5 from the sums and differences of the pairs (1, 4) and
     // (2, 3): y1,4 = a1 -+ sign i b1 and y2,3 = a2 -+ sign i b2 with
     // a1 = x0 + c1 t1 + c2 t2, a2 = x0 + c2 t1 + c1 t2,
     // b1 = s1 d1 + s2 d2, b2 = s2 d1 - s1 d2 (c_n, s_n = cos, sin 2 pi n / 5)
-    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr], x3 = src[j + 3 * nr], x4 = src[j + 4 * nr];
+    cpx<T> x0 = src[sw<T>(j)], x1 = src[sw<T>(j + nr)], x2 = src[sw<T>(j + 2 * nr)], x3 = src[sw<T>(j + 3 * nr)],
+           x4 = src[sw<T>(j + 4 * nr)];
     if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); x3 = cmul(x3, w3); x4 = cmul(x4, w4); }
     const T c1 = (T)0.30901699437494742410229341718281906, c2 = (T)-0.80901699437494742410229341718281906;
     const T s1 = (T)0.95105651629515357211643933337938214, s2 = (T)0.58778525229247312916870595463907277;
@@ -123,13 +140,13 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
     // e = b * (-sign i): forward (-i) b = (b.y, -b.x), backward (+i) b = (-b.y, b.x)
     const cpx<T> e1 = BACKWARD ? mk<T>(-b1.y, b1.x) : mk<T>(b1.y, -b1.x);
     const cpx<T> e2 = BACKWARD ? mk<T>(-b2.y, b2.x) : mk<T>(b2.y, -b2.x);
-    dst[base] = cadd(x0, cadd(t1, t2));
-    dst[base + ns] = cadd(a1, e1);
-    dst[base + 2 * ns] = cadd(a2, e2);
-    dst[base + 3 * ns] = csub(a2, e2);
-    dst[base + 4 * ns] = csub(a1, e1);
+    dst[sw<T>(base)] = cadd(x0, cadd(t1, t2));
+    dst[sw<T>(base + ns)] = cadd(a1, e1);
+    dst[sw<T>(base + 2 * ns)] = cadd(a2, e2);
+    dst[sw<T>(base + 3 * ns)] = csub(a2, e2);
+    dst[sw<T>(base + 4 * ns)] = csub(a1, e1);
   } else {  // R == 3
-    cpx<T> x0 = src[j], x1 = src[j + nr], x2 = src[j + 2 * nr];
+    cpx<T> x0 = src[sw<T>(j)], x1 = src[sw<T>(j + nr)], x2 = src[sw<T>(j + 2 * nr)];
     if (twid) { x1 = cmul(x1, w1); x2 = cmul(x2, w2); }
     const T s60 = (T)0.86602540378443864676372317075294;
     const cpx<T> t = cadd(x1, x2);
@@ -137,9 +154,9 @@ __device__ __forceinline__ void butterfly(const cpx<T> *src, cpx<T> *dst, int R,
     const cpx<T> m = mk<T>(x0.x - (T)0.5 * t.x, x0.y - (T)0.5 * t.y);
     // u = d * (sign i sin60)
     const cpx<T> u = BACKWARD ? mk<T>(-s60 * d.y, s60 * d.x) : mk<T>(s60 * d.y, -s60 * d.x);
-    dst[base] = cadd(x0, t);
-    dst[base + ns] = cadd(m, u);
-    dst[base + 2 * ns] = csub(m, u);
+    dst[sw<T>(base)] = cadd(x0, t);
+    dst[sw<T>(base + ns)] = cadd(m, u);
+    dst[sw<T>(base + 2 * ns)] = csub(m, u);
   }
 }
 

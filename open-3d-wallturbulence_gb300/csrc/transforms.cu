@@ -48,7 +48,7 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
-  const int ls = d.NZ2 + 1;
+  const int ls = line_stride<T>(d.NZ2);
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + TX * ls;
   const int i0 = bx * TX;
@@ -62,7 +62,7 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
     const int kz = idx / TX, c = idx - kz * TX;
     if (i0 + c < d.NXH && kz != d.NZH && !(a.mean_split && kz == 0 && i0 + c == 0)) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
-      bufa[c * ls + slot] = from_d<T>(src[(size_t)kz * d.NXH + i0 + c]);
+      bufa[c * ls + sw<T>(slot)] = from_d<T>(src[(size_t)kz * d.NXH + i0 + c]);
     }
   }
   __syncthreads();
@@ -70,7 +70,7 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
   cpx<T> *dst = reinterpret_cast<cpx<T> *>(a.zbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
     const int z = idx / TX, c = idx - z * TX;
-    if (i0 + c < d.NXH) dst[(size_t)z * d.NXH + i0 + c] = r[c * ls + z];
+    if (i0 + c < d.NXH) dst[(size_t)z * d.NXH + i0 + c] = r[c * ls + sw<T>(z)];
   }
 }
 
@@ -78,7 +78,7 @@ template <typename T, int P, bool R5>
 __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
-  const int ls = d.NX2 + 1;
+  const int ls = line_stride<T>(d.NX2);
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + 3 * P * ls;
   const size_t nlines = (size_t)d.NY * d.NZ2;
@@ -107,7 +107,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
         z = mk<T>(x.x + y.y, y.x - x.y);
       }
     }
-    bufa[q * ls + mm] = z;
+    bufa[q * ls + sw<T>(mm)] = z;
   }
   __syncthreads();
   const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.twx);
@@ -116,7 +116,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   // 2. lamb = u x omega, packed as (lx + i ly) per line and (lz_l + i lz_l+1)
 #pragma unroll
   for (int l = 0; l < P; ++l) {
-    const int x = mm;
+    const int x = sw<T>(mm);
     const cpx<T> uv = r[(0 * P + l) * ls + x], wox = r[(1 * P + l) * ls + x], oyz = r[(2 * P + l) * ls + x];
     const T u = uv.x, v = uv.y, w = wox.x, ox = wox.y, oy = oyz.x, oz = oyz.y;
     const T lx = mul_rn(v, oz) - mul_rn(w, oy);
@@ -137,13 +137,13 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
     if (line >= nlines) continue;
     const int mc = (km == 0) ? 0 : d.NX2 - km;
     {
-      const cpx<T> zm = fo[l * ls + km], zc = fo[l * ls + mc];
+      const cpx<T> zm = fo[l * ls + sw<T>(km)], zc = fo[l * ls + sw<T>(mc)];
       // Xa = (Z[m] + conj Z[-m]) / 2 ; Xb = (Z[m] - conj Z[-m]) / (2i)
       lb[line * d.NXH + km] = mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
       lb[fstride + line * d.NXH + km] = mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half);
     }
     {
-      const cpx<T> zm = fo[(P + l / 2) * ls + km], zc = fo[(P + l / 2) * ls + mc];
+      const cpx<T> zm = fo[(P + l / 2) * ls + sw<T>(km)], zc = fo[(P + l / 2) * ls + sw<T>(mc)];
       const cpx<T> val = (l & 1) ? mk<T>((zm.y + zc.y) * half, (zc.x - zm.x) * half)
                                  : mk<T>((zm.x + zc.x) * half, (zm.y - zc.y) * half);
       lb[2 * fstride + line * d.NXH + km] = val;
@@ -156,14 +156,14 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
   constexpr int TX = XCfg<T>::TX;
   extern __shared__ __align__(16) unsigned char smraw[];
   const XformDims d = a.d;
-  const int ls = d.NZ2 + 1;
+  const int ls = line_stride<T>(d.NZ2);
   cpx<T> *bufa = reinterpret_cast<cpx<T> *>(smraw);
   cpx<T> *bufb = bufa + TX * ls;
   const int i0 = bx * TX;
   const cpx<T> *src = reinterpret_cast<const cpx<T> *>(a.lbuf) + ((size_t)f * d.NY + j) * d.NZ2 * d.NXH;
   for (int idx = threadIdx.x; idx < d.NZ2 * TX; idx += blockDim.x) {
     const int z = idx / TX, c = idx - z * TX;
-    bufa[c * ls + z] = (i0 + c < d.NXH) ? src[(size_t)z * d.NXH + i0 + c] : mk<T>((T)0, (T)0);
+    bufa[c * ls + sw<T>(z)] = (i0 + c < d.NXH) ? src[(size_t)z * d.NXH + i0 + c] : mk<T>((T)0, (T)0);
   }
   __syncthreads();
   const cpx<T> *r = fft_lines<T, false, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
@@ -177,7 +177,7 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
     const int kz = idx / TX, c = idx - kz * TX;
     if (i0 + c < d.NXH) {
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
-      const double2 v = to_d(r[c * ls + slot]);
+      const double2 v = to_d(r[c * ls + sw<T>(slot)]);
       const size_t at = (size_t)kz * d.NXH + i0 + c;
       double2 o = make_double2(v.x * sc, v.y * sc);
       if (kSplit && lm) {
@@ -317,9 +317,9 @@ static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
 }
 
 template <typename T>
-static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * (d.NZ2 + 1) * sizeof(cpx<T>); }
+static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * line_stride<T>(d.NZ2) * sizeof(cpx<T>); }
 template <typename T>
-static size_t smem_x(const XformDims &d, int P) { return 2 * 3 * (size_t)P * (d.NX2 + 1) * sizeof(cpx<T>); }
+static size_t smem_x(const XformDims &d, int P) { return 2 * 3 * (size_t)P * line_stride<T>(d.NX2) * sizeof(cpx<T>); }
 // (y, z) lines per x block: XCfg<T>::P where its shared memory fits, else 2
 // (FP64 lines longer than 604 points)
 template <typename T>
