@@ -85,7 +85,9 @@ inline bool make_fft_plan(int L, const int *radices, int nst, FftPlan &p) {
 // i ^ 5 ((i >> 4) & 3): the stride-R stores of the first two radix-4 stages
 // then hit 16 different bank pairs per half-warp instead of 4, and runs of
 // consecutive points stay conflict-free.  A line occupies whole blocks
-// (line_stride).  FP64 lines are stored as they are.
+// (line_stride).  FP64 lines are stored as they are: the same permutation
+// over blocks of 8 (i ^ (g | (g & 2) << 1)) removes their conflicts too but
+// measured slower, the FP64 kernels being FP64-pipe-bound.
 template <typename T>
 __device__ __forceinline__ int sw(int i) {
   if (sizeof(T) == sizeof(float)) return i ^ (5 * ((i >> 4) & 3));
