@@ -55,3 +55,21 @@ def test_null_handle_calls_fail_cleanly(gpu_lib):
     assert lib.owt_time_integration(None, 1) == 1
     assert lib.owt_synchronize(None) == 1
     assert lib.owt_destroy(None) == 0
+
+
+def test_batch_seeded_and_selftest_entry_points_refuse_bad_arguments_without_a_gpu(gpu_lib):
+    from owt import lib as L
+    lib = L.load(gpu_lib)
+    b = C.c_void_p()
+    assert lib.owt_batch_create(None, 0, C.byref(b)) == L.OK + 1
+    assert b.value is None and "at least one handle" in lib.owt_last_error(None).decode()
+    assert lib.owt_batch_step(None, 1) == L.OK + 1
+    assert lib.owt_batch_destroy(None) == L.OK
+    assert lib.owt_batch_tuning_report(None) == b""
+    assert lib.owt_init_seeded(None, 1, 0.1) == L.OK + 1
+    assert lib.owt_setup_report(None) == b""
+    bad, t1, t2 = C.c_int64(0), C.c_float(0), C.c_float(0)
+    # band widths the library does not use, and empty systems, are refused before any device work
+    assert lib.owt_band_factor_selftest(3, 3, 10, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
+    assert lib.owt_band_factor_selftest(15, 13, 0, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
+    assert "bad arguments" in lib.owt_last_error(None).decode()
