@@ -93,6 +93,7 @@ struct owt_handle {
   cudaGraph_t graph = nullptr;
   bool q_dirty[3] = {false, false, false};
   bool sparse_v = false;        // interior fill of every v-system inside the masks
+  bool sparse_v6 = false;       // the same against the sixth-order masks (fd_order 6)
   int pattern_violations = 0;   // modes that forced the dense solve
   Grid grid;
   double Ly = 0, inv_cg0 = 0;
@@ -280,18 +281,18 @@ struct owt_handle {
     phase("band factorizations");
     // interior fill of both systems inside the compile-time masks? then the
     // masked solves apply
-    sparse_v = false;
+    sparse_v = sparse_v6 = false;
     // (systems shorter than the two edges have no masked blocks: full band)
     if (bv.n % 4 == 0 && bg.n % 2 == 0) {
       int *d_bad = dalloc<int>(2, owned);
       ck(cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st), "memset");
-      launch_check_pattern(0, bv.ab, bv.piv, bv.n, Uq, d_bad, st);
+      launch_check_pattern(p.fd_order == 6 ? 2 : 0, bv.ab, bv.piv, bv.n, Uq, d_bad, st);
       launch_check_pattern(1, bg.ab, bg.piv, bg.n, Uq, d_bad + 1, st);
       launches += 2;
       int nbad[2] = {0, 0};
       ck(cudaMemcpyAsync(nbad, d_bad, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "pattern check");
       ck(cudaStreamSynchronize(st), "pattern check");
-      sparse_v = (nbad[0] == 0 && nbad[1] == 0);
+      (p.fd_order == 6 ? sparse_v6 : sparse_v) = (nbad[0] == 0 && nbad[1] == 0);
       pattern_violations = nbad[0] + nbad[1];
     }
     phase("pattern check");
@@ -473,6 +474,10 @@ struct owt_handle {
     launches += 4 + nx;
   }
   void stage_modes() {
+    if (sparse_v6 && !force_dense) {
+      launch_modes_sixth(mode_args(), st);
+      return;
+    }
     launch_modes(mode_args(), bv.kl, bv.ku, bg.kl, bg.ku, modes_sparse(),
                  forced_variant >= 0 ? forced_variant : modes_variant, st);
   }
@@ -584,6 +589,7 @@ struct owt_handle {
   void autotune_modes() {
     modes_variant = 0;
     tuning.clear();
+    if (sparse_v6) { tuning = "sixth-order masked solve (one variant)"; return; }
     if (!sparse_v) { tuning = "full-band solve (no variants)"; return; }
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
@@ -1712,7 +1718,7 @@ const char *owt_setup_report(const owt_handle *h) { return h ? h->setup_report.c
 int owt_get_info(const owt_handle *h, int what, int64_t *value) {
   if (!h || !value) return OWT_ERR_INVALID;
   switch (what) {
-    case OWT_INFO_SPARSE_SOLVE: *value = (h->sparse_v && !h->force_dense) ? 1 : 0; return OWT_OK;
+    case OWT_INFO_SPARSE_SOLVE: *value = ((h->sparse_v || h->sparse_v6) && !h->force_dense) ? 1 : 0; return OWT_OK;
     case OWT_INFO_PATTERN_VIOLATIONS: *value = h->pattern_violations; return OWT_OK;
     case OWT_INFO_DEVICE_BYTES: *value = (int64_t)h->device_bytes; return OWT_OK;
     case OWT_INFO_MODES_VARIANT: *value = h->forced_variant >= 0 ? h->forced_variant : h->modes_variant; return OWT_OK;

@@ -22,7 +22,7 @@ namespace owt {
 //     interior equations were substituted)
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
 // ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD>
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, class VM = VMasks>
 __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
   // One thread per real component of a mode (the band systems are real).
   // Pair mapping: lanes 2m, 2m+1 are Re, Im of mode m.  Quad mapping: lanes
@@ -178,15 +178,15 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
         }
       }
     };
-    if (SPARSE) band_solve_v_sparse(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    if (SPARSE) band_solve_v_sparse<VM>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
     else band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
   }
 }
 
 // One channel: thread tid of the grid is thread tid of the mapping.
-template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB>
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB, class VM = VMasks>
 __global__ void __launch_bounds__(BLOCK, MINB) k_modes(const __grid_constant__ ModeArgs a) {
-  mode_body<KLV, KUV, KLG, KUG, SPARSE, QUAD>(a, blockIdx.x * BLOCK + threadIdx.x);
+  mode_body<KLV, KUV, KLG, KUG, SPARSE, QUAD, VM>(a, blockIdx.x * BLOCK + threadIdx.x);
 }
 
 // Every channel of a batch in one persistent launch.  Work items are the
@@ -223,6 +223,7 @@ int modes_pair_count();
 const char *modes_pair_name(int v);
 void modes_pair_launch(int v, const ModeArgs &a, cudaStream_t st);
 void modes_dense_launch(const ModeArgs &a, cudaStream_t st);
+void modes_sixth_launch(const ModeArgs &a, cudaStream_t st);  // the sixth-order masks
 int modes_quad_count();
 const char *modes_quad_name(int v);
 void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st);

@@ -40,6 +40,13 @@ void modes_dense_launch(const ModeArgs &a, cudaStream_t st) {
   k_modes<15, 13, 6, 6, false, false, 128, 3><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
 }
 
+// masked solve with the sixth-order fill (one variant: the sixth-order option
+// is not autotuned)
+void modes_sixth_launch(const ModeArgs &a, cudaStream_t st) {
+  const int bs = 128;
+  k_modes<15, 13, 6, 6, true, false, 128, 3, VMasks6><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
+}
+
 ModeBatchShape modes_pair_batch_shape(int v) {
   const Variant &x = kVariants[v];
   return {x.block, false, resident(x.batch, x.block)};

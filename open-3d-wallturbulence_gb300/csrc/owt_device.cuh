@@ -338,6 +338,22 @@ struct VMasks {
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask_p(ty); }
 };
+// The sixth-order option (fd_order = 6) fills differently; its masks come
+// from the same derivation over the same sweep.
+__host__ __device__ constexpr unsigned long long vmask6_l(int ty) {
+  return ty == 0 ? 0xcffeull : ty == 1 ? 0x67feull : ty == 2 ? 0x33feull : 0x19feull;
+}
+__host__ __device__ constexpr unsigned long long vmask6_u(int ty) {
+  return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1ffeull : 0x3feull;
+}
+__host__ __device__ constexpr unsigned long long vmask6_p(int ty) {
+  return ty == 0 ? 0x5eull : ty == 1 ? 0x1eull : ty == 2 ? 0x12ull : 0x8cull;
+}
+struct VMasks6 {
+  __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask6_l(ty); }
+  __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask6_u(ty); }
+  __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask6_p(ty); }
+};
 struct GMasks {
   __host__ __device__ static constexpr unsigned long long l(int ty) { return gmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return gmask_u(ty); }
@@ -420,11 +436,12 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
   }
 }
 
-template <class Rhs, class YStore, class YLoad, class Out>
+// VM: VMasks (the reference's eighth-order operators) or VMasks6
+template <class VM = VMasks, class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<15, 13, 4, 2, 16, 32, VB_EDGE, VMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<15, 13, 4, 2, 16, 32, VB_EDGE, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,

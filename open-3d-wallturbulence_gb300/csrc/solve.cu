@@ -354,13 +354,18 @@ __global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__
 }
 
 // which: 0 the v-system, 1 the omega_y-system
+// which: 0 the v-system against the eighth-order masks, 1 the omega_y-system,
+// 2 the v-system against the sixth-order masks
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
                           cudaStream_t st) {
   if (which == 0)
     k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+  else if (which == 2)
+    k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks6><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
   else
     k_check_pattern<6, 6, 2, 0, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
 }
+void launch_modes_sixth(const ModeArgs &a, cudaStream_t st) { modes_sixth_launch(a, st); }
 
 __global__ void k_advance(long long *step) { *step += 1; }
 void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>>>(step); }

@@ -140,6 +140,7 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
                         const double *t2, const double *s1, const double *s2, double *rscale, int *info,
                         cudaStream_t st, int kernel = 0);
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
+void launch_modes_sixth(const ModeArgs &a, cudaStream_t st);  // masked solve with the sixth-order fill
 int modes_variant_count();
 const char *modes_variant_name(int v);
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,

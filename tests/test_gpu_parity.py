@@ -318,7 +318,10 @@ def test_sixth_order_steps_match_oracle(gpu_lib, port_lib, size):
         o.set_velocity(u, v, w)
         g = gpu_solver(p)
         g.init_fields(u, v, w)
-        print(size, "sparse solve:", g.info("sparse_solve"), "pattern violations:", g.info("pattern_violations"))
+        print(size, "sparse solve:", g.info("sparse_solve"), "pattern violations:", g.info("pattern_violations"),
+              g.tuning_report())
+        if size == "128x129x128":  # the sixth-order masks hold for the Re_tau=180 case
+            assert g.info("sparse_solve") == 1
         compare_state(g, o, 1e-11, tag=f"order 6 {size} init")
         for s in range(nsteps):
             g.time_Integration(1)

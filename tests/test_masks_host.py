@@ -1,8 +1,9 @@
 """The interior fill and pivot masks compiled into the masked band solves
-(vmask_*, gmask_* in csrc/owt_device.cuh) are the ones the derivation
-program (csrc/masks/derive_masks.cpp) finds from the production band
-templates of the reference's eighth-order operators: built with g++ and run
-here, its output must equal the compiled constants."""
+(vmask_*, vmask6_*, gmask_* in csrc/owt_device.cuh) are the ones the
+derivation program (csrc/masks/derive_masks.cpp) finds from the production
+band templates of the reference's eighth-order operators and of the
+sixth-order option: built with g++ and run here, its output must equal the
+compiled constants."""
 import os
 import re
 import subprocess
@@ -48,9 +49,10 @@ def _compiled():
                 return int(val, 16)
         return int(parts[-1], 16)
     v = {k: [eval_mask(masks(f"vmask_{k.lower()}"), ty) for ty in range(4)] for k in ("L", "U", "P")}
+    v6 = {k: [eval_mask(masks(f"vmask6_{k.lower()}"), ty) for ty in range(4)] for k in ("L", "U", "P")}
     g = [eval_mask(masks("gmask_l"), 0), eval_mask(masks("gmask_l"), 1),
          eval_mask(masks("gmask_u"), 0), eval_mask(masks("gmask_u"), 1)]
-    return v, g
+    return v, v6, g
 
 
 def test_compiled_masks_are_the_derived_ones():
@@ -58,7 +60,10 @@ def test_compiled_masks_are_the_derived_ones():
         text = _derive()
     except (OSError, subprocess.CalledProcessError) as e:  # no g++
         pytest.skip(f"cannot build the derivation program: {e}")
+    want_v, want_v6, want_g = _compiled()
     got_v, got_g = _order_block(text, 8)
-    want_v, want_g = _compiled()
     assert got_v == want_v
     assert got_g == want_g
+    got_v6, got_g6 = _order_block(text, 6)  # the sixth-order option: its own v masks, the same g masks
+    assert got_v6 == want_v6
+    assert got_g6 == want_g
