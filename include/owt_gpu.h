@@ -308,10 +308,11 @@ int owt_drag_backward(owt_handle *h, double grad_objective, double *grad_bottom,
 
 /* DY1 along y for device arrays the caller owns, allocating no device memory.
  * No counterpart in the reference: it is the compact first derivative of
- * owt_dy_apply (order 1), out = diag(c11) A1^-1 B1 in, for callers that must
- * not call cudaMalloc -- code running during CUDA graph capture, programs
- * whose own pool allocator owns all device memory, and loops that cannot
- * afford cudaMalloc's device-wide synchronisation.  It needs no handle.
+ * owt_dy_apply (order 1), out = diag(c11) A1^-1 B1 in, for callers that cannot
+ * call cudaMalloc: programs whose own pool allocator owns the device memory
+ * and forbids allocations from elsewhere, and loops that cannot accept the
+ * implicit device-wide synchronisation of cudaMalloc/cudaFree.  It needs no
+ * handle (creating one allocates).
  *  - d_in, d_out: device pointers, 16-byte aligned, NY * nlines complex128
  *    (interleaved), line index fastest: [y][line] (a whole field in the
  *    library's device layout is nlines = NZ * NX/2).
@@ -322,11 +323,13 @@ int owt_drag_backward(owt_handle *h, double grad_objective, double *grad_bottom,
  *    OWT_NOALLOC_MAX_NY or NY * nlines <= OWT_NOALLOC_MAX_VALUES are rejected
  *    with OWT_ERR_INVALID and a message in owt_last_error(NULL).
  *  - The first call on a device looks up that array's device address (once
- *    per device, with the device current); make that first call before any
- *    stream capture.
- *  - Every call rewrites everything it reads from the array (operators,
- *    then scratch) before using it; calls share the array, so calls that can
- *    overlap on the GPU (different streams without ordering) race.
+ *    per device, with the device current) and keeps it; make that first call
+ *    before any stream capture, and do not use the entry point across a
+ *    cudaDeviceReset, which invalidates the kept address.
+ *  - Every call rebuilds the operator tables it reads (then the scratch) for
+ *    its own (NY, alpha_mesh) before using them; calls share the one array,
+ *    so calls that can overlap on the GPU (different streams without
+ *    ordering between them) race and give wrong results.
  *  - Asynchronous on `stream` (a cudaStream_t, NULL for the legacy default
  *    stream); errors of the launch are returned, device-side ones appear at
  *    the caller's next synchronisation. */

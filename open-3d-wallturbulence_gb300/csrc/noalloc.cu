@@ -1,26 +1,27 @@
 // DY1 along y for caller-owned device arrays, without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
-// being captured (allocation is not a stream operation), host programs that
-// hand the whole device memory to their own pool allocator and forbid other
-// allocations, and tight loops where cudaMalloc's implicit device-wide
-// synchronisation is not acceptable.  owt_dy1_noalloc serves them: it needs no
-// handle (creating one allocates) and keeps its scratch in a file-scope
-// static __device__ array of fixed size.  That array is reserved on every GPU
-// that loads this library, for the life of the process.
+// Some callers cannot call cudaMalloc: programs that hand the whole device
+// memory to their own pool allocator and forbid allocations from elsewhere,
+// and tight loops that cannot accept the implicit device-wide
+// synchronisation cudaMalloc and cudaFree bring.  owt_dy1_noalloc serves
+// them: it needs no handle (creating one allocates) and keeps its scratch in
+// a file-scope static __device__ array of fixed size.  That array is reserved
+// on every GPU that loads this library, for the life of the process.
 //
 // What it computes is the handle-based DY1 (owt_dy_apply with order 1):
 // out = diag(c11) A1^-1 B1 in along y, for every line, with the compact first
 // derivative of src/compdiff.hpp:11-69 and c11 = 1/(dy/ds) of
 // src/solver.cpp:77,94 on the grid y = tanh(alpha s)/tanh(alpha).  Each call
 // first rebuilds the A1 band factors, B1 rows and c11 for its (NY, alpha) in
-// the static array (one small kernel), then runs the derivative kernel.
+// the static array (one small kernel, noalloc_setup.h), then runs the
+// derivative kernel.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <mutex>
 #include <string>
 
+#include "noalloc_setup.h"
 #include "owt_device.cuh"
 #include "owt_gpu.h"
 
@@ -28,95 +29,19 @@ namespace owt {
 
 // Layout of the static array: [setup region][bf: MAX values][yscr: MAX values]
 constexpr size_t NOALLOC_SETUP_BYTES = 256 * 1024;
+static_assert(noalloc_setup_bytes() <= NOALLOC_SETUP_BYTES, "setup tables exceed their region");
+static_assert(kNoallocMaxNY == OWT_NOALLOC_MAX_NY, "table layout and the entry point's limit disagree");
 constexpr size_t NOALLOC_SCRATCH_BYTES =
     NOALLOC_SETUP_BYTES + 2 * (size_t)OWT_NOALLOC_MAX_VALUES * sizeof(double2);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-struct NoallocSetup {
-  // all inside the setup region; NY <= OWT_NOALLOC_MAX_NY
-  double *ab;      // 7 x NY band (kl = ku = 2, LAPACK factorization layout)
-  uint8_t *piv;    // NY
-  double *c11;     // NY
-  int *bcol;       // NY x 5
-  double *bval;    // NY x 5
-};
-
-__host__ __device__ inline NoallocSetup noalloc_layout(unsigned char *base, int NY) {
-  NoallocSetup s;
-  const int nmax = OWT_NOALLOC_MAX_NY;
-  s.ab = reinterpret_cast<double *>(base);
-  s.c11 = s.ab + 7 * nmax;
-  s.bval = s.c11 + nmax;
-  s.bcol = reinterpret_cast<int *>(s.bval + 5 * nmax);
-  s.piv = reinterpret_cast<uint8_t *>(s.bcol + 5 * nmax);
-  (void)NY;
-  return s;
-}
-
-// One thread: grid metric, B1 rows, A1 band assembled and factored with
-// partial pivoting (the dgbtf2 order used by the handle's factorization).
-// Everything the derivative kernel reads is rewritten here, band fill rows
-// cleared, so nothing depends on what an earlier call left in the array.
+// One thread builds the operator tables for (NY, alpha) in the array.
 __global__ void k_noalloc_setup(unsigned char *base, int NY, double alpha) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  NoallocSetup s = noalloc_layout(base, NY);
-  const double h = 2.0 / (NY - 1.0);
-  const double coth_ap = 1.0 / tanh(alpha);
-  for (int i = 0; i < NY; ++i) {
-    const double si = 2 * i / (NY - 1.0) - 1.0;
-    const double sech = 1.0 / cosh(alpha * si);
-    s.c11[i] = 1.0 / (alpha * coth_ap * sech * sech);
-  }
-  // B1 rows (col, val) x 5, zero-padded
-  for (int e = 0; e < 5 * NY; ++e) { s.bcol[e] = 0; s.bval[e] = 0.0; }
-  auto put = [&](int row, int k, int col, double v) { s.bcol[row * 5 + k] = col; s.bval[row * 5 + k] = v; };
-  const double a2 = 40.0 / 27.0, b2 = 25.0 / 54.0;
-  for (int i = 2; i < NY - 2; ++i) {
-    put(i, 0, i - 2, -b2 / (4 * h)); put(i, 1, i - 1, -a2 / (2 * h));
-    put(i, 2, i + 1, a2 / (2 * h)); put(i, 3, i + 2, b2 / (4 * h));
-  }
-  for (int i : {1, NY - 2}) { put(i, 0, i - 1, -1.5 / (2 * h)); put(i, 1, i + 1, 1.5 / (2 * h)); }
-  const double a0 = -17.0 / 6.0, b0 = 1.5, c0 = 1.5, d0 = -1.0 / 6.0;
-  put(0, 0, 0, a0 / h); put(0, 1, 1, b0 / h); put(0, 2, 2, c0 / h); put(0, 3, 3, d0 / h);
-  put(NY - 1, 0, NY - 1, -a0 / h); put(NY - 1, 1, NY - 2, -b0 / h);
-  put(NY - 1, 2, NY - 3, -c0 / h); put(NY - 1, 3, NY - 4, -d0 / h);
-  // A1 band, rows b = KV + i - j with KV = 4 (kl = ku = 2)
-  constexpr int KL = 2, KU = 2, KV = KL + KU, NB = 2 * KL + KU + 1;
-  for (int e = 0; e < NB * NY; ++e) s.ab[e] = 0.0;
-  auto A = [&](int i, int j) -> double & { return s.ab[(KV + i - j) * NY + j]; };
-  for (int i = 2; i < NY - 2; ++i) {
-    A(i, i - 2) = 1.0 / 36.0; A(i, i - 1) = 4.0 / 9.0; A(i, i) = 1.0; A(i, i + 1) = 4.0 / 9.0; A(i, i + 2) = 1.0 / 36.0;
-  }
-  for (int i : {1, NY - 2}) { A(i, i - 1) = 0.25; A(i, i) = 1.0; A(i, i + 1) = 0.25; }
-  A(0, 0) = 1.0; A(0, 1) = 3.0; A(NY - 1, NY - 1) = 1.0; A(NY - 1, NY - 2) = 3.0;
-  auto AB = [&](int b, int c) -> double & { return s.ab[b * NY + c]; };
-  int ju = 0;
-  for (int j = 0; j < NY; ++j) {
-    const int km = min(KL, NY - 1 - j);
-    int jp = 0;
-    double best = fabs(AB(KV, j));
-    for (int i = 1; i <= km; ++i) {
-      const double v = fabs(AB(KV + i, j));
-      if (v > best) { best = v; jp = i; }
-    }
-    s.piv[j] = (uint8_t)jp;
-    ju = max(ju, min(j + KU + jp, NY - 1));
-    if (jp != 0)
-      for (int c = j; c <= ju; ++c) {
-        const double t = AB(KV + jp - (c - j), c);
-        AB(KV + jp - (c - j), c) = AB(KV - (c - j), c);
-        AB(KV - (c - j), c) = t;
-      }
-    const double rp = 1.0 / AB(KV, j);
-    for (int i = 1; i <= km; ++i) AB(KV + i, j) *= rp;
-    for (int c = j + 1; c <= ju; ++c) {
-      const double t = AB(KV - (c - j), c);
-      if (t != 0.0)
-        for (int i = 1; i <= km; ++i) AB(KV + i - (c - j), c) -= AB(KV + i, j) * t;
-    }
-  }
-  for (int j = 0; j < NY; ++j) AB(KV, j) = 1.0 / AB(KV, j);
+  const NoallocSetup s = noalloc_layout(base);
+  noalloc_assemble(s, NY, alpha);
+  noalloc_factor(s, NY);
 }
 
 // One thread per line: bf = B1 f, band solve with A1, out = c11 * d.
@@ -124,7 +49,7 @@ __global__ void __launch_bounds__(128) k_dy1_noalloc(unsigned char *base, int NY
                                                      const double2 *__restrict__ in, double2 *__restrict__ out) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nlines) return;
-  NoallocSetup s = noalloc_layout(base, NY);
+  const NoallocSetup s = noalloc_layout(base);
   double2 *bf = reinterpret_cast<double2 *>(base + NOALLOC_SETUP_BYTES);
   double2 *yscr = bf + OWT_NOALLOC_MAX_VALUES;
   const int M = nlines;
@@ -154,8 +79,12 @@ __global__ void __launch_bounds__(128) k_dy1_noalloc(unsigned char *base, int NY
 void owt_set_thread_error(const std::string &m);
 
 namespace {
+// Device address of the static array, looked up once per device on the first
+// call with that device current.  It belongs to the device's primary context:
+// after cudaDeviceReset it would be stale, so this entry point must not be
+// used across a device reset.
 std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_ptr[256] = {nullptr};  // device address of the static array, per device
+unsigned char *g_noalloc_ptr[256] = {nullptr};
 }  // namespace
 
 extern "C" int owt_dy1_noalloc(int64_t NY, int64_t nlines, double alpha_mesh, const double *d_in, double *d_out,
