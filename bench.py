@@ -97,10 +97,12 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# algorithmic work per stage (fixed formulas; see the design doc for derivations)
+# algorithmic work per stage (fixed formulas, derived from the kernels' loops)
 # ---------------------------------------------------------------------------
 def stage_work(p, precision="fp64"):
-    """Algorithmic flops and bytes per launch of each kernel."""
+    """Algorithmic flops and bytes per launch of each kernel: band solves as LAPACK counts
+    them, FFTs at 5 N log2 N, 9 flops per physical point for the products, and the
+    spectral fields / z-padded planes each kernel must read and write once."""
     import math
     NY, M, NXH, NZ2, NX2 = p.NY, p.NZ * p.NXH, p.NXH, p.NZ2, p.NX2
     S = 16.0 * NY * M  # bytes per spectral field (complex128)
@@ -121,7 +123,8 @@ def stage_work(p, precision="fp64"):
 
 
 # DRAM traffic per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-# of the 128x129x128 workload (profiles/k_xlamb_k_modes_channel180.md), scaled to
+# of the 128x129x128 workload (profiles/k_xlamb_k_zback_channel180.md and
+# profiles/k_modes_channel180.md), scaled to
 # a launch at another size by the units the kernel processes (traffic grows in
 # proportion: y-z lines times kx modes for the transforms, modes times NY for the
 # mode kernel).

@@ -317,8 +317,9 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 constexpr int VB_EDGE = 48;
 constexpr int GB_EDGE = 60;
 // v-system (v, d1, d2, d3 per interior node): 26.25 entries per column
-// instead of 43 (the reference's operators; the sixth-order option fills
-// differently and runs the full band)
+// instead of 43 (the reference's eighth-order operators; the sixth-order
+// option has masks of its own, vmask6_* / VMasks6 below, checked at setup by
+// launch_check_pattern with type 2)
 __host__ __device__ constexpr unsigned long long vmask_l(int ty) {
   return ty == 0 ? 0x3ffeull : ty == 1 ? 0x1ffeull : ty == 2 ? 0xffeull : 0x7feull;
 }

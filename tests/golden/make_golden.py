@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
 Run where the reference sources exist (it needs ``oracle/_ref/libowt_ref.so``,
-built by ``make -C oracle ref``): the reference's own src/solver.cpp,
+built by ``make -C oracle ref REF_SRC=<reference>/src``): the reference's own src/solver.cpp,
 src/FFT.cpp and src/parallel.cpp, compiled unmodified against the oracle's
 MPI/FFTW/LAPACK shims.  The fixtures are small .npz files; the tests compare the
 CPU restatement (oracle/owt_port.cpp) and the CUDA path against them.

@@ -439,7 +439,7 @@ def test_reference_retau550_case_size_lamb_vector_and_steps(gpu_lib):
     kx = np.arange(NXH) * p.dkx
     kz = np.where(np.arange(NZ) < p.NZH, np.arange(NZ), np.arange(NZ) - NZ) * p.dkz
     K = np.sqrt(kx[None, :] ** 2 + kz[:, None] ** 2)
-    amp = np.where(K > 0, (np.maximum(K, 1e-300) / 0.5) ** -2.0, 0.0) * 0.05
+    amp = np.where(K > 0, (np.maximum(K, 0.5 * p.dkx) / 0.5) ** -2.0, 0.0) * 0.05
     y = np.tanh(p.alpha_mesh * np.linspace(-1, 1, NY)) / np.tanh(p.alpha_mesh)
     shape = (1 - y ** 2)
 
