@@ -1,0 +1,384 @@
+// The time step of a handle: the launch sequence of one step
+// (src/solver.cpp:541-627) and its CUDA graph, the mode-kernel autotuner,
+// the reference routines run one at a time, init_fields, and the layout
+// transposes of host <-> device copies.
+#include "handle.h"
+
+using namespace owt;
+
+void owt_handle::dapply(int order, const double2 *in, double2 *out) {
+  DApplyArgs a{};
+  a.NY = NY; a.M = M; a.in = in; a.out = out;
+  const BandDev &b = order == 1 ? b1 : b2;
+  a.ab = b.ab; a.piv = b.piv;
+  a.b_col = order == 1 ? b1_col : b2_col;
+  a.b_val = order == 1 ? b1_val : b2_val;
+  a.bf = bf; a.yscr = yscr;
+  launch_dapply(a, st);
+  ++launches;
+}
+
+XformArgs owt_handle::xform_args() const {
+  XformArgs a{};
+  a.d = XformDims{NY, NZ, NXH, NZH, NX2, NZ2};
+  a.in[0] = u; a.in[1] = v_ring; a.in[2] = w; a.in[3] = ox; a.in[4] = g_ring; a.in[5] = oz;
+  a.ring_mask = (1 << 1) | (1 << 4);
+  a.fs = fs;
+  a.step = d_step;
+  a.mean_split = precision == OWT_PREC_MIXED ? 1 : 0;
+  for (int f = 0; f < 3; ++f) a.lm[f] = lm + (size_t)f * fs;
+  a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
+  a.zbuf = zbuf; a.lbuf = lbuf;
+  a.px = px; a.pz = pz;
+  a.twx = twx[precision]; a.twz = twz[precision];
+  a.inv_nx2 = 1.0 / (double)NX2; a.inv_nz2 = 1.0 / (double)NZ2;
+  return a;
+}
+
+NLArgs owt_handle::nl_args(bool record_mean) const {
+  NLArgs a{};
+  a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.M = M;
+  a.kx = kx; a.kz = kz; a.c11 = c11;
+  a.lx = lx; a.ly = ly; a.lz = lz;
+  a.hv_ring = hv_ring; a.hg_ring = hg_ring;
+  a.ab1 = b1.ab; a.piv1 = b1.piv; a.b1_col = b1_col; a.b1_val = b1_val;
+  a.yscr = yscr;
+  a.lx_mean = record_mean ? lxm_ring : nullptr;
+  a.lz_mean = record_mean ? lzm_ring : nullptr;
+  a.step = d_step;
+  return a;
+}
+
+// One time step.  Every argument is a fixed device pointer; which ring slot
+// is which history level is read from the device step counter, so the same
+// launch sequence (or its CUDA graph) serves every step.
+// The mean mode runs on a second stream beside the mode kernel (they touch
+// disjoint data); both read the counter before it advances.
+void owt_handle::enqueue_step() {
+  ck(cudaEventRecord(ev_fork, st), "fork");
+  ck(cudaStreamWaitEvent(st2, ev_fork, 0), "fork wait");
+  stage_mean(true, st2);
+  ck(cudaEventRecord(ev_join, st2), "join");
+  stage_modes();
+  ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
+  launch_advance(d_step, st);
+  const XformArgs xa = xform_args();
+  int nx = 3;
+  if (xa.mean_split) {
+    // the FP64 mean-flow terms beside the FP32 z backward and x pass
+    ck(cudaEventRecord(ev_fork2, st), "fork");
+    ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
+    launch_lamb_part(xa, precision, 3, st2);
+    ck(cudaEventRecord(ev_join2, st2), "join");
+    launch_lamb_part(xa, precision, 0, st);
+    launch_lamb_part(xa, precision, 1, st);
+    ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
+    launch_lamb_part(xa, precision, 2, st);
+    nx = 4;
+  } else {
+    nx = launch_lamb(xa, precision, st);
+  }
+  launch_nl(nl_args(true), st);
+  launches += 4 + nx;
+}
+
+void owt_handle::stage_modes() {
+  if (sparse_v6 && !force_dense) {
+    launch_modes_sixth(mode_args(), st);
+    return;
+  }
+  launch_modes(mode_args(), bv.kl, bv.ku, bg.kl, bg.ku, modes_sparse(),
+               forced_variant >= 0 ? forced_variant : modes_variant, st);
+}
+
+ModeArgs owt_handle::mode_args() const {
+  ModeArgs a{};
+  a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.U = Uq;
+  a.inv_dt = 1.0 / p.dt; a.nu = p.nu;
+  a.kx = kx; a.kz = kz; a.c11 = c11; a.c21 = c21; a.c22 = c22;
+  a.v_ring = v_ring; a.g_ring = g_ring; a.hv_ring = hv_ring; a.hg_ring = hg_ring; a.q_ring = q_ring;
+  a.u_out = u; a.w_out = w; a.ox_out = ox; a.oz_out = oz;
+  a.ab_v = bv.ab; a.piv_v = bv.piv; a.n_v = bv.n;
+  a.ab_g = bg.ab; a.piv_g = bg.piv; a.n_g = bg.n;
+  a.rhs_node_v = rhs_node_v; a.rb_col = rb_col; a.rb_val = rb_val; a.inv_cg = inv_cg;
+  a.rs_v = bv.rscale; a.rs_g = bg.rscale;
+  a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
+  a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg; a.sv = sv;
+  a.rbv_col = rbv_col; a.rbv_val = rbv_val;
+  a.nc21 = nc21; a.nc22 = nc22;
+  a.step = d_step;
+  a.vw = vw_on ? vw : nullptr;
+  return a;
+}
+
+void owt_handle::stage_mean(bool pre_advance, cudaStream_t s) {
+  launch_mean(mean_args(pre_advance), mean_smem, s ? s : st);
+}
+
+MeanArgs owt_handle::mean_args(bool pre_advance) const {
+  MeanArgs ma{};
+  ma.pre_advance = pre_advance ? 1 : 0;
+  ma.NY = NY; ma.M = M; ma.U = Uq; ma.n_g = bg.n;
+  ma.inv_dt = 1.0 / p.dt; ma.nu = p.nu; ma.Ly = Ly; ma.inv_cg0 = inv_cg0;
+  ma.c11 = c11; ma.c21 = c21; ma.c22 = c22;
+  ma.ab_g = bg.ab; ma.piv_g = bg.piv; ma.rb_col = rb_col; ma.rb_val = rb_val;
+  ma.rs_g = bg.rscale; ma.inv_h = 1.0 / grid.ds; ma.inv_h2 = 1.0 / (grid.ds * grid.ds);
+  ma.U_ring = U_ring; ma.W_ring = W_ring; ma.lx_ring = lxm_ring; ma.lz_ring = lzm_ring;
+  ma.fx_ring = fx_ring; ma.fz_ring = fz_ring;
+  ma.u_field = u; ma.w_field = w; ma.ox_field = ox; ma.oz_field = oz;
+  ma.scratch = mean_scratch; ma.dy1 = mean_dy1; ma.step = d_step; ma.err = d_err;
+  return ma;
+}
+
+void owt_handle::run_steps(int64_t n) {
+  ensure_tuned();
+  recompute_dirty_q();
+  if (use_graph) {
+    if (!gexec) {
+      ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+      const int64_t before = launches;
+      enqueue_step();
+      per_step_launches = launches - before;
+      launches = before;
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      ck(e, "end capture");
+      ck(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+    }
+    for (int64_t s = 0; s < n; ++s) {
+      ck(cudaGraphLaunch(gexec, st), "graph launch");
+      launches += per_step_launches;
+      ++steps;
+    }
+  } else {
+    for (int64_t s = 0; s < n; ++s) {
+      enqueue_step();
+      ++steps;
+    }
+  }
+  check_launch("time step");
+}
+
+void owt_handle::ensure_tuned() {
+  if (tuned) return;
+  tuned = true;
+  if (!initialized) {
+    autotune_modes();
+    return;
+  }
+  recompute_dirty_q();
+  double2 *snap = nullptr;
+  ck(cudaMalloc(&snap, 13 * fs * sizeof(double2)), "tuning snapshot");
+  try {
+    double2 *o = snap;
+    for (double2 *ring : {v_ring, g_ring, q_ring}) { d2d(o, ring, 3 * fs * sizeof(double2)); o += 3 * fs; }
+    for (double2 *f : {u, w, ox, oz}) { d2d(o, f, fs * sizeof(double2)); o += fs; }
+    autotune_modes();
+    o = snap;
+    for (double2 *ring : {v_ring, g_ring, q_ring}) { d2d(ring, o, 3 * fs * sizeof(double2)); o += 3 * fs; }
+    for (double2 *f : {u, w, ox, oz}) { d2d(f, o, fs * sizeof(double2)); o += fs; }
+    ck(cudaStreamSynchronize(st), "tuning restore");
+  } catch (...) {
+    cudaStreamSynchronize(st);
+    cudaFree(snap);
+    throw;
+  }
+  cudaFree(snap);
+}
+
+void owt_handle::autotune_modes() {
+  modes_variant = 0;
+  tuning.clear();
+  if (sparse_v6) { tuning = "sixth-order masked solve (one variant)"; return; }
+  if (!sparse_v) { tuning = "full-band solve (no variants)"; return; }
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  float best = 1e30f;
+  for (int v = 0; v < modes_variant_count(); ++v) {
+    forced_variant = v;
+    stage_modes();  // warm-up
+    ck(cudaEventRecord(e0, st), "event");
+    for (int r = 0; r < 2; ++r) stage_modes();
+    ck(cudaEventRecord(e1, st), "event");
+    ck(cudaEventSynchronize(e1), "event");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+    ms *= 0.5f;
+    launches += 3;
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "%s%s=%.3fms", tuning.empty() ? "" : " ", modes_variant_name(v), ms);
+    tuning += buf;
+    if (ms < best) { best = ms; modes_variant = v; }
+  }
+  forced_variant = -1;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  check_launch("autotune");
+  tuning += std::string(" -> ") + modes_variant_name(modes_variant);
+}
+
+// DY2 v for history levels whose v was replaced from the host (one launch).
+void owt_handle::recompute_dirty_q() {
+  DY2Args a{};
+  a.NY = NY; a.M = M;
+  a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
+  a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
+  a.c21 = c21; a.c22 = c22;
+  double2 *scr[3] = {tmpA, tmpB, tmpC};
+  for (int sl = 0; sl < 3; ++sl) {
+    if (!q_dirty[sl]) continue;
+    a.in[a.nf] = v_ring + (size_t)sl * fs;
+    a.out[a.nf] = q_ring + (size_t)sl * fs;
+    a.scr[a.nf] = scr[a.nf];
+    ++a.nf;
+    q_dirty[sl] = false;
+  }
+  if (!a.nf) return;
+  launch_dy2(a, st);
+  ++launches;
+}
+
+void owt_handle::copy_ring(double2 *ring, size_t n, int from, int to) {
+  ck(cudaMemcpyAsync(ring + (size_t)to * n, ring + (size_t)from * n, n * sizeof(double2), cudaMemcpyDeviceToDevice,
+                     st), "ring copy");
+}
+
+// column of mode 0 of a device-layout field -> contiguous NY vector
+void owt_handle::mode0_column(double2 *dst, const double2 *field) {
+  ck(cudaMemcpy2DAsync(dst, sizeof(double2), field, (size_t)M * sizeof(double2), sizeof(double2), NY,
+                       cudaMemcpyDeviceToDevice, st), "mode-0 column");
+}
+
+void owt_handle::get_vor_from_vel() {
+  dapply(1, u, tmpA);
+  dapply(1, w, tmpB);
+  VorArgs va{};
+  va.NY = NY; va.NXH = NXH; va.M = M; va.kx = kx; va.kz = kz; va.c11 = c11;
+  va.u = u; va.v = ring_level(v_ring, 0); va.w = w; va.d1u = tmpA; va.d1w = tmpB;
+  va.ox = ox; va.oy = ring_level(g_ring, 0); va.oz = oz;
+  launch_vor(va, st);
+  ++launches;
+}
+
+void owt_handle::lamb_vec(bool explicit_shift) {
+  launches += launch_lamb(xform_args(), precision, st);
+  if (explicit_shift) {
+    launch_lamb_mean_shift(lxm_ring, lzm_ring, lx, lz, NY, M, d_step, st);
+    ++launches;
+  }
+}
+
+void owt_handle::nonlinear_source(bool record_mean) {
+  launch_nl(nl_args(record_mean), st);
+  ++launches;
+}
+
+void owt_handle::friction(int shift) {
+  dapply(1, u, tmpA);
+  dapply(1, w, tmpB);
+  launch_friction(tmpA, tmpB, c11, NY, M, p.nu, Ly, fx_ring, fz_ring, d_step, shift, d_err, st);
+  ++launches;
+}
+
+void owt_handle::init_prologue() {
+  steps = 0;
+  drop_graph();
+  ck(cudaMemsetAsync(d_step, 0, sizeof(long long), st), "memset");
+  ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "memset");
+}
+
+void owt_handle::init_fields(const double *hu, const double *hv, const double *hw) {
+  init_prologue();
+  to_device(hu, u);
+  to_device(hv, ring_level(v_ring, 0));
+  to_device(hw, w);
+  init_from_velocity();
+}
+
+// The seeded laminar + random divergence-free state, generated on the
+// device (seeded_ic.cu); the Chebyshev coefficients live in the mean-flow
+// buffer and omega_y in tmpC until the velocity is complete.
+void owt_handle::init_seeded(uint64_t seed, double rms) {
+  init_prologue();
+  SeedArgs a{};
+  a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.degree = 5;
+  a.seed = seed;
+  a.kmin = std::min(p.dkx, p.dkz);
+  a.kx = kx; a.kz = kz; a.y = ygrid; a.c11 = c11; a.wy = wy;
+  a.coef = lm;  // 3 NY M >= 12 M values
+  double2 *v0 = ring_level(v_ring, 0);
+  launches += launch_ic_fields(a, v0, tmpC, st);
+  dapply(1, v0, tmpA);
+  launches += launch_ic_velocity(a, tmpA, tmpC, u, v0, w, ic_partial, rms, st);
+  check_launch("seeded initial condition");
+  init_from_velocity();
+}
+
+void owt_handle::init_from_velocity() {
+  get_vor_from_vel();  // also leaves D1 u, D1 w in tmpA, tmpB
+  launch_friction(tmpA, tmpB, c11, NY, M, p.nu, Ly, fx_ring, fz_ring, d_step, 0, d_err, st);
+  ++launches;
+  lamb_vec(false);
+  nonlinear_source(true);
+  const int s0 = slot(0);
+  for (double2 *ring : {v_ring, g_ring, hv_ring, hg_ring})
+    for (int l = 1; l < 3; ++l) copy_ring(ring, fs, s0, slot(l));
+  for (double2 *ring : {lxm_ring, lzm_ring})
+    for (int l = 1; l < 3; ++l) copy_ring(ring, NY, s0, slot(l));
+  mode0_column(U_ring + (size_t)s0 * NY, u);
+  mode0_column(W_ring + (size_t)s0 * NY, w);
+  for (double2 *ring : {U_ring, W_ring})
+    for (int l = 1; l < 3; ++l) copy_ring(ring, NY, s0, slot(l));
+  for (double *fr : {fx_ring, fz_ring})
+    for (int l = 1; l < 3; ++l)
+      ck(cudaMemcpyAsync(fr + slot(l), fr + s0, sizeof(double), cudaMemcpyDeviceToDevice, st), "fric copy");
+  q_dirty[0] = q_dirty[1] = q_dirty[2] = true;
+  recompute_dirty_q();
+  check_launch("init_fields");
+  initialized = true;
+}
+
+void owt_handle::to_device(const double *host, double2 *dst) {
+  ck(cudaMemcpyAsync(stage, host, fs * sizeof(double2), cudaMemcpyHostToDevice, st), "H2D");
+  launch_transpose(stage, dst, M, NY, st);  // [M][NY] -> [NY][M]
+  ++launches;
+  check_launch("layout transpose");
+}
+
+void owt_handle::to_host(const double2 *src, double *host) {
+  launch_transpose(src, stage, NY, M, st);  // [NY][M] -> [M][NY]
+  ++launches;
+  check_launch("layout transpose");
+  ck(cudaMemcpyAsync(host, stage, fs * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H");
+  ck(cudaStreamSynchronize(st), "D2H");
+}
+
+double2 *owt_handle::field_ptr(int f, bool for_write) {
+  switch (f) {
+    case OWT_VELX: return u;
+    case OWT_VELZ: return w;
+    case OWT_VORX: return ox;
+    case OWT_VORZ: return oz;
+    case OWT_LMBX: return lx;
+    case OWT_LMBY: return ly;
+    case OWT_LMBZ: return lz;
+    case OWT_VELY: case OWT_VELY_0: case OWT_VELY_1: case OWT_VELY_2: {
+      const int l = f == OWT_VELY ? 0 : f - OWT_VELY_0;
+      if (for_write) q_dirty[slot(l)] = true;
+      return ring_level(v_ring, l);
+    }
+    case OWT_VORY: return ring_level(g_ring, 0);
+    case OWT_VORY_0: case OWT_VORY_1: case OWT_VORY_2: return ring_level(g_ring, f - OWT_VORY_0);
+    case OWT_HV: return ring_level(hv_ring, 0);
+    case OWT_HV_0: case OWT_HV_1: case OWT_HV_2: return ring_level(hv_ring, f - OWT_HV_0);
+    case OWT_HG: return ring_level(hg_ring, 0);
+    case OWT_HG_0: case OWT_HG_1: case OWT_HG_2: return ring_level(hg_ring, f - OWT_HG_0);
+    default: throw OwtError(OWT_ERR_INVALID, "unknown field id " + std::to_string(f));
+  }
+}
+
+double2 *owt_handle::mean_ptr(int which) {
+  if (which < 0 || which >= OWT_NUM_MEANS) throw OwtError(OWT_ERR_INVALID, "unknown mean id");
+  double2 *rings[4] = {lxm_ring, lzm_ring, U_ring, W_ring};
+  return rings[which / 3] + (size_t)slot(which % 3) * NY;
+}
