@@ -173,6 +173,19 @@ int owt_get_launch_count(const owt_handle *h, int64_t *count);
 int owt_get_grid(const owt_handle *h, double *y);
 int owt_dy_apply(owt_handle *h, int order, const double *in, double *out);
 
+/* Fourier2Physical_dealiased (src/FFT.cpp:49-128) and
+ * Physical2Fourier_dealiased (src/FFT.cpp:130-194) of one field, in FP64
+ * whatever the handle's precision, with the step's own transform kernels:
+ * spec is [z][x][y] complex128 (NZ * NX/2 * NY values), phys is the
+ * reference's Field<double> on the 3/2 grid, [z][x][y] with z in [0, 3NZ/2),
+ * x in [0, 3NX/2): 3NZ/2 * 3NX/2 * NY doubles.  The Nyquist-z row is dropped
+ * on the way to physical space and kept on the way back, kx = 0 enters
+ * through its real part, the forward result is scaled by 1/(NX2 NZ2), as
+ * the reference does.  The handle's state is not changed; a temporary device
+ * buffer of two physical fields is allocated for the call. */
+int owt_fourier2physical(owt_handle *h, const double *spec, double *phys);
+int owt_physical2fourier(owt_handle *h, const double *phys, double *spec);
+
 /* Batches of independent channels (no counterpart in the reference, which runs
  * one channel per MPI job).  A batch step is one CUDA graph launch in which
  * every kernel of the time step runs once over all channels (one launch per

@@ -330,4 +330,18 @@ int owt_dy_apply(owt_handle *h, int order, const double *in, double *out) {
   });
 }
 
+int owt_fourier2physical(owt_handle *h, const double *spec, double *phys) {
+  return guard(h, [&] {
+    if (!spec || !phys) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    h->fourier2physical(spec, phys);
+  });
+}
+
+int owt_physical2fourier(owt_handle *h, const double *phys, double *spec) {
+  return guard(h, [&] {
+    if (!spec || !phys) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    h->physical2fourier(phys, spec);
+  });
+}
+
 }  // extern "C"

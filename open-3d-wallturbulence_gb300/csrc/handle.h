@@ -209,6 +209,11 @@ struct owt_handle {
   void to_device(const double *host, double2 *dst);
   void to_host(const double2 *src, double *host);
   double2 *field_ptr(int f, bool for_write);
+  // The reference's stand-alone dealiased transforms of one field, FP64:
+  // spectral [z][x][y] complex128 <-> physical [z][x][y] doubles on the 3/2
+  // grid (src/FFT.cpp:49-194); temporary device buffers for the physical field.
+  void fourier2physical(const double *spec, double *phys);
+  void physical2fourier(const double *phys, double *spec);
   double2 *mean_ptr(int which);
   // ---- wall-drag adjoint -------------------------------------------------------
   // Objective J = (1/N) sum_{n=1..N} fx_n over the N steps of a forward run,

@@ -245,6 +245,7 @@ void owt_handle::setup(const owt_params &prm) {
   mean_dy1 = dalloc<double2>(2 * (size_t)NY, owned);
   XformDims xd{NY, NZ, NXH, NZH, NX2, NZ2};
   ck(lamb_prepare(xd), "transform kernel attributes");
+  ck(phys_prepare(xd), "transform kernel attributes");
   mean_smem = mean_prepare(NY, bg.n);
   zbuf = dalloc<unsigned char>(lamb_zbuf_bytes(xd, 0), owned);
   lbuf = dalloc<unsigned char>(lamb_lbuf_bytes(xd, 0), owned);

@@ -382,3 +382,57 @@ double2 *owt_handle::mean_ptr(int which) {
   double2 *rings[4] = {lxm_ring, lzm_ring, U_ring, W_ring};
   return rings[which / 3] + (size_t)slot(which % 3) * NY;
 }
+
+// FP64 tables whatever the handle's precision; no mean split; field 0 of the
+// transform buffers; the state fields are not touched.
+static XformArgs phys_args(const owt_handle &h) {
+  XformArgs a = h.xform_args();
+  a.ring_mask = 0;
+  a.mean_split = 0;
+  a.twx = h.twx[0];
+  a.twz = h.twz[0];
+  return a;
+}
+
+void owt_handle::fourier2physical(const double *spec, double *phys) {
+  const size_t np = (size_t)NZ2 * NX2 * NY;
+  std::vector<void *> tmp;
+  try {
+    double *dphys = dalloc<double>(2 * np, tmp);
+    to_device(spec, tmpC);
+    XformArgs a = phys_args(*this);
+    a.in[0] = tmpC;
+    launch_fourier2physical(a, dphys, st);
+    launch_transpose_real(dphys, dphys + np, NY, NZ2 * NX2, st);  // [y][z][x] -> [z][x][y]
+    launches += 3;
+    check_launch("fourier2physical");
+    ck(cudaMemcpyAsync(phys, dphys + np, np * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "fourier2physical");
+  } catch (...) {
+    cudaStreamSynchronize(st);
+    for (void *q : tmp) cudaFree(q);
+    throw;
+  }
+  for (void *q : tmp) cudaFree(q);
+}
+
+void owt_handle::physical2fourier(const double *phys, double *spec) {
+  const size_t np = (size_t)NZ2 * NX2 * NY;
+  std::vector<void *> tmp;
+  try {
+    double *dphys = dalloc<double>(2 * np, tmp);
+    ck(cudaMemcpyAsync(dphys + np, phys, np * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+    launch_transpose_real(dphys + np, dphys, NZ2 * NX2, NY, st);  // [z][x][y] -> [y][z][x]
+    XformArgs a = phys_args(*this);
+    a.out[0] = tmpC;
+    launch_physical2fourier(a, dphys, st);
+    launches += 3;
+    check_launch("physical2fourier");
+    to_host(tmpC, spec);
+  } catch (...) {
+    cudaStreamSynchronize(st);
+    for (void *q : tmp) cudaFree(q);
+    throw;
+  }
+  for (void *q : tmp) cudaFree(q);
+}

@@ -821,5 +821,24 @@ void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaS
   dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
   k_transpose<<<g, b, 0, st>>>(in, out, rows, cols);
 }
+// Physical fields: [y][z][x] (device) <-> [z][x][y] (the reference's
+// Field<double> layout), a rows x cols transpose of doubles.
+__global__ void k_transpose_real(const double *__restrict__ in, double *__restrict__ out, int rows, int cols) {
+  __shared__ double tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = by + r, col = bx + threadIdx.x;
+    if (row < rows && col < cols) tile[r][threadIdx.x] = in[(size_t)row * cols + col];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int orow = bx + r, ocol = by + threadIdx.x;
+    if (orow < cols && ocol < rows) out[(size_t)orow * rows + ocol] = tile[threadIdx.x][r];
+  }
+}
+void launch_transpose_real(const double *in, double *out, int rows, int cols, cudaStream_t st) {
+  dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose_real<<<g, b, 0, st>>>(in, out, rows, cols);
+}
 
 }  // namespace owt

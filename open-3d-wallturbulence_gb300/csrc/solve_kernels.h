@@ -159,6 +159,8 @@ void launch_friction(const double2 *d1u, const double2 *d1w, const double *c11, 
 void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
                             const long long *step, cudaStream_t st);
 void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st);
+// the same for a rows x cols matrix of doubles
+void launch_transpose_real(const double *in, double *out, int rows, int cols, cudaStream_t st);
 void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,
                   cudaStream_t st);
 
@@ -170,6 +172,11 @@ int launch_lamb(const XformArgs &a, int precision, cudaStream_t st);
 cudaError_t lamb_prepare(const XformDims &d);
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st);
 size_t lamb_zbuf_bytes(const XformDims &d, int precision);
+// Stand-alone FP64 dealiased transforms of one field (zbuf / lbuf field 0 in
+// between): a.in[0] -> phys [y][z][x], and phys -> a.out[0].
+cudaError_t phys_prepare(const XformDims &d);
+void launch_fourier2physical(const XformArgs &a, double *phys, cudaStream_t st);
+void launch_physical2fourier(const XformArgs &a, const double *phys, cudaStream_t st);
 size_t lamb_lbuf_bytes(const XformDims &d, int precision);
 
 // Seeded initial condition (seeded_ic.cu): Chebyshev coefficients per mode

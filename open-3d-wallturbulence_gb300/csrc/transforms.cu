@@ -74,6 +74,28 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
   }
 }
 
+// Point mm of the complex line whose backward FFT is a + i b, for the
+// spectra A, B (kx = 0 .. NXH-1) of two real lines: Hermitian extension in x
+// (slot i = u_i, slot NX2 - i = conj u_i, FFT.cpp:109-119), the imaginary
+// part of u_0 ignored (the real part of the reference's c2c output), slots
+// NXH .. NX2-NXH zero (padding).  MAYBE_NO_B: B may be null (b = 0).
+template <typename T, bool MAYBE_NO_B = false>
+__device__ __forceinline__ cpx<T> hermitian_pair(const cpx<T> *A, const cpx<T> *B, int mm, int NXH, int NX2) {
+  const cpx<T> zero = mk<T>((T)0, (T)0);
+  const bool hb = !MAYBE_NO_B || B != nullptr;
+  if (mm == 0) return mk<T>(A[0].x, hb ? B[0].x : (T)0);
+  if (mm < NXH) {
+    const cpx<T> x = A[mm], y = hb ? B[mm] : zero;
+    return mk<T>(x.x - y.y, x.y + y.x);
+  }
+  if (mm > NX2 - NXH) {
+    const int mp = NX2 - mm;
+    const cpx<T> x = A[mp], y = hb ? B[mp] : zero;
+    return mk<T>(x.x + y.y, y.x - x.y);
+  }
+  return zero;
+}
+
 template <typename T, int P, bool R5>
 __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -95,17 +117,7 @@ __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
     cpx<T> z = mk<T>((T)0, (T)0);
     if (line < nlines) {
       const cpx<T> *A = zb + (size_t)(2 * pair) * fstride + line * d.NXH;
-      const cpx<T> *B = A + fstride;
-      if (mm == 0) {
-        z = mk<T>(A[0].x, B[0].x);
-      } else if (mm < d.NXH) {
-        const cpx<T> x = A[mm], y = B[mm];
-        z = mk<T>(x.x - y.y, x.y + y.x);
-      } else if (mm > d.NX2 - d.NXH) {
-        const int mp = d.NX2 - mm;
-        const cpx<T> x = A[mp], y = B[mp];
-        z = mk<T>(x.x + y.y, y.x - x.y);
-      }
+      z = hermitian_pair<T>(A, A + fstride, mm, d.NXH, d.NX2);
     }
     bufa[q * ls + sw<T>(mm)] = z;
   }
@@ -281,6 +293,69 @@ __global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ Xform
   mean_lamb_body(a, blockIdx.x, blockIdx.y);
 }
 
+// Stand-alone dealiased transforms of one field in FP64 (the reference's
+// Fourier2Physical_dealiased / Physical2Fourier_dealiased, src/FFT.cpp:49-194):
+// the z passes are the step's (field 0 of zbuf / lbuf); these x kernels write
+// or read physical lines instead of forming products.  A block transforms
+// 2 kPhysQ (y, z) lines, two real lines per complex FFT; physical lines are
+// [y][z][x] with x fastest.
+constexpr int kPhysQ = 4;
+template <bool R5>
+__global__ void __launch_bounds__(1024) k_xback_phys(const __grid_constant__ XformArgs a, double *phys) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const XformDims d = a.d;
+  const int ls = line_stride<double>(d.NX2);
+  double2 *bufa = reinterpret_cast<double2 *>(smraw);
+  double2 *bufb = bufa + kPhysQ * ls;
+  const size_t nlines = (size_t)d.NY * d.NZ2;
+  const size_t line0 = (size_t)blockIdx.x * 2 * kPhysQ;
+  const double2 *zb = reinterpret_cast<const double2 *>(a.zbuf);
+  const int mm = threadIdx.x;
+  for (int q = 0; q < kPhysQ; ++q) {
+    const size_t la = line0 + 2 * q, lb = la + 1;
+    double2 z = make_double2(0.0, 0.0);
+    if (la < nlines)
+      z = hermitian_pair<double, true>(zb + la * d.NXH, lb < nlines ? zb + lb * d.NXH : nullptr, mm, d.NXH, d.NX2);
+    bufa[q * ls + mm] = z;
+  }
+  __syncthreads();
+  const double2 *r = fft_lines<double, true, R5>(bufa, bufb, kPhysQ, ls, a.px, reinterpret_cast<const double2 *>(a.twx));
+  for (int q = 0; q < kPhysQ; ++q) {
+    const size_t la = line0 + 2 * q, lb = la + 1;
+    const double2 v = r[q * ls + mm];
+    if (la < nlines) phys[la * d.NX2 + mm] = v.x;
+    if (lb < nlines) phys[lb * d.NX2 + mm] = v.y;
+  }
+}
+template <bool R5>
+__global__ void __launch_bounds__(1024) k_xfwd_phys(const __grid_constant__ XformArgs a, const double *phys) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const XformDims d = a.d;
+  const int ls = line_stride<double>(d.NX2);
+  double2 *bufa = reinterpret_cast<double2 *>(smraw);
+  double2 *bufb = bufa + kPhysQ * ls;
+  const size_t nlines = (size_t)d.NY * d.NZ2;
+  const size_t line0 = (size_t)blockIdx.x * 2 * kPhysQ;
+  const int mm = threadIdx.x;
+  for (int q = 0; q < kPhysQ; ++q) {
+    const size_t la = line0 + 2 * q, lb = la + 1;
+    bufa[q * ls + mm] = make_double2(la < nlines ? phys[la * d.NX2 + mm] : 0.0, lb < nlines ? phys[lb * d.NX2 + mm] : 0.0);
+  }
+  __syncthreads();
+  const double2 *fo = fft_lines<double, false, R5>(bufa, bufb, kPhysQ, ls, a.px, reinterpret_cast<const double2 *>(a.twx));
+  // keep kx < NXH, / NX2 (FFT.cpp:153-162): Xa = (Z[m] + conj Z[-m]) / 2, Xb = (Z[m] - conj Z[-m]) / (2i)
+  double2 *lb_out = reinterpret_cast<double2 *>(a.lbuf);
+  const double half = 0.5 * a.inv_nx2;
+  for (int idx = threadIdx.x; idx < kPhysQ * d.NXH; idx += blockDim.x) {
+    const int q = idx / d.NXH, km = idx - q * d.NXH;
+    const size_t la = line0 + 2 * q, lb = la + 1;
+    const int mc = (km == 0) ? 0 : d.NX2 - km;
+    const double2 zm = fo[q * ls + km], zc = fo[q * ls + mc];
+    if (la < nlines) lb_out[la * d.NXH + km] = make_double2((zm.x + zc.x) * half, (zm.y - zc.y) * half);
+    if (lb < nlines) lb_out[lb * d.NXH + km] = make_double2((zm.y + zc.y) * half, (zc.x - zm.x) * half);
+  }
+}
+
 // Batched: one launch over every channel of a table whose channels share the
 // precision and the length of the lines a block spans (NZ2 for the z passes,
 // NX2 for the x pass); blocks are numbered channel by channel, each channel's
@@ -447,6 +522,40 @@ static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t 
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_batch_t<double>(t, part, st);
   else lamb_batch_t<float>(t, part, st);
+}
+
+static size_t smem_phys(const XformDims &d) { return 2 * (size_t)kPhysQ * line_stride<double>(d.NX2) * sizeof(double2); }
+
+cudaError_t phys_prepare(const XformDims &d) {
+  const size_t sx = smem_phys(d);
+  cudaError_t e = raise_smem_limit(k_xback_phys<true>, sx);
+  if (e == cudaSuccess) e = raise_smem_limit(k_xback_phys<false>, sx);
+  if (e == cudaSuccess) e = raise_smem_limit(k_xfwd_phys<true>, sx);
+  if (e == cudaSuccess) e = raise_smem_limit(k_xfwd_phys<false>, sx);
+  return e;
+}
+
+// a.in[0] (spectral [y][kz][kx], FP64 tables) -> phys [y][z][x]; zbuf field 0 in between.
+void launch_fourier2physical(const XformArgs &a, double *phys, cudaStream_t st) {
+  const XformDims &d = a.d;
+  const XformKernels<double> k = kernels<double>(d);
+  constexpr int TX = XCfg<double>::TX;
+  k.zback<<<dim3((d.NXH + TX - 1) / TX, d.NY, 1), d.NZ2, smem_z<double>(d), st>>>(a);
+  const size_t nl = (size_t)d.NY * d.NZ2;
+  const unsigned blocks = (unsigned)((nl + 2 * kPhysQ - 1) / (2 * kPhysQ));
+  if (d.NX2 % 5 == 0) k_xback_phys<true><<<blocks, d.NX2, smem_phys(d), st>>>(a, phys);
+  else k_xback_phys<false><<<blocks, d.NX2, smem_phys(d), st>>>(a, phys);
+}
+// phys [y][z][x] -> a.out[0] (spectral); lbuf field 0 in between.
+void launch_physical2fourier(const XformArgs &a, const double *phys, cudaStream_t st) {
+  const XformDims &d = a.d;
+  const XformKernels<double> k = kernels<double>(d);
+  constexpr int TX = XCfg<double>::TX;
+  const size_t nl = (size_t)d.NY * d.NZ2;
+  const unsigned blocks = (unsigned)((nl + 2 * kPhysQ - 1) / (2 * kPhysQ));
+  if (d.NX2 % 5 == 0) k_xfwd_phys<true><<<blocks, d.NX2, smem_phys(d), st>>>(a, phys);
+  else k_xfwd_phys<false><<<blocks, d.NX2, smem_phys(d), st>>>(a, phys);
+  k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 1), d.NZ2, smem_z<double>(d), st>>>(a);
 }
 
 size_t lamb_zbuf_bytes(const XformDims &d, int precision) {

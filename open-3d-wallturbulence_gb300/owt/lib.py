@@ -72,6 +72,8 @@ def load(path=LIB):
         "owt_get_launch_count": ([_h, C.POINTER(C.c_int64)], C.c_int),
         "owt_get_grid": ([_h, _dp], C.c_int),
         "owt_dy_apply": ([_h, C.c_int, _dp, _dp], C.c_int),
+        "owt_fourier2physical": ([_h, _dp, _dp], C.c_int),
+        "owt_physical2fourier": ([_h, _dp, _dp], C.c_int),
         "owt_enqueue_stage": ([_h, C.c_int], C.c_int),
         "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),
         "owt_get_info": ([_h, C.c_int, C.POINTER(C.c_int64)], C.c_int),

@@ -132,6 +132,27 @@ class GpuSolver:
         self._chk(self.L.owt_dy_apply(self.h, int(order), _L.dptr(a.view(np.float64)), _L.dptr(out.view(np.float64))))
         return out
 
+    @property
+    def physical_shape(self):
+        p = self.params
+        return (p.NZ2, p.NX2, p.NY)
+
+    def Fourier2Physical_dealiased(self, u):
+        """src/FFT.cpp:49-128 on one field: [z][x][y] complex -> [z2][x2][y] real."""
+        a = self._c(u)
+        out = np.empty(self.physical_shape)
+        self._chk(self.L.owt_fourier2physical(self.h, _L.dptr(a.view(np.float64)), _L.dptr(out)))
+        return out
+
+    def Physical2Fourier_dealiased(self, up):
+        """src/FFT.cpp:130-194 on one field: [z2][x2][y] real -> [z][x][y] complex."""
+        a = np.ascontiguousarray(up, dtype=np.float64)
+        if a.shape != self.physical_shape:
+            raise ValueError(f"expected shape {self.physical_shape}, got {a.shape}")
+        out = np.empty(self.shape, np.complex128)
+        self._chk(self.L.owt_physical2fourier(self.h, _L.dptr(a), _L.dptr(out.view(np.float64))))
+        return out
+
     def grid(self):
         y = np.empty(self.params.NY)
         self._chk(self.L.owt_get_grid(self.h, _L.dptr(y)))
