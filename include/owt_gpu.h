@@ -237,6 +237,14 @@ int owt_state_restore(owt_handle *h);
  * OWT_OPT_FORCE_DENSE_BANDS: 1 = sweep the full band of the v-system in every
  *   column instead of skipping structurally-zero interior entries (the two
  *   give the same result; this exists to test that).
+ * OWT_OPT_FFT_STOCKHAM: 1 = the mixed precision's FP32 transforms use the
+ *   shared-memory Stockham kernels (one pass per radix-2/3/4/5 stage) even
+ *   where register-transform kernels exist for the line length (the two
+ *   agree to FP32 rounding; this exists to compare them).
+ * OWT_OPT_MEAN_SPLIT: mixed precision only; 1 (the default) = the FP32
+ *   transforms carry the fluctuations and the mean-flow terms of the Lamb
+ *   vector (mean velocity x fluctuating vorticity and back) are formed in FP64
+ *   spectrally beside them; 0 = the FP32 transforms carry the whole fields.
  * OWT_INFO_SPARSE_SOLVE: 1 if the interior-sparse v-system solve is active.
  * OWT_INFO_PATTERN_VIOLATIONS: modes whose factors fell outside the sparse
  *   pattern at setup (any such mode selects the full-band solve).
@@ -248,6 +256,8 @@ int owt_state_restore(owt_handle *h);
  * (-1 returns to the tuned choice), owt_tuning_report() lists the timings. */
 #define OWT_OPT_FORCE_DENSE_BANDS 1
 #define OWT_OPT_MODES_VARIANT 2
+#define OWT_OPT_FFT_STOCKHAM 3
+#define OWT_OPT_MEAN_SPLIT 4
 #define OWT_INFO_SPARSE_SOLVE 1
 #define OWT_INFO_PATTERN_VIOLATIONS 2
 #define OWT_INFO_DEVICE_BYTES 3

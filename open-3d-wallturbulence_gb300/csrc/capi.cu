@@ -237,6 +237,10 @@ int owt_set_option(owt_handle *h, int option, int64_t value) {
     h->drop_graph();
     if (option == OWT_OPT_FORCE_DENSE_BANDS) {
       h->force_dense = value != 0;
+    } else if (option == OWT_OPT_FFT_STOCKHAM) {
+      h->fft_stockham = value != 0;
+    } else if (option == OWT_OPT_MEAN_SPLIT) {
+      h->mean_split = value != 0;
     } else if (option == OWT_OPT_MODES_VARIANT) {
       if (value < -1 || value >= modes_variant_count()) throw OwtError(OWT_ERR_INVALID, "no such variant");
       h->forced_variant = (int)value;

@@ -1,6 +1,8 @@
 // Batches of channels (owt_batch_*): every kernel of the step launched once
 // over all channels of a group, the mode kernel as one persistent launch,
 // the whole batch step as one CUDA graph.
+#include <tuple>
+
 #include "handle.h"
 
 using namespace owt;
@@ -133,20 +135,20 @@ struct owt_batch {
     std::vector<XformArgs> xargs;
     for (owt_handle *h : hs) xargs.push_back(h->xform_args());
     for (int part = 0; part < 4; ++part) {
-      std::map<std::pair<int, int>, std::vector<int>> groups;
+      std::map<std::tuple<int, int, int>, std::vector<int>> groups;  // (precision, line length, Stockham kernels)
       std::vector<int> blocks(n, 0);
       for (int i = 0; i < n; ++i) {
         const owt_handle *h = hs[i];
-        if (part == 3 && h->precision != OWT_PREC_MIXED) continue;
+        if (part == 3 && !xargs[i].mean_split) continue;
         const XformDims &d = xargs[i].d;
         const int prec = h->precision == OWT_PREC_MIXED ? 1 : 0;
         if (part == 0) ck(lamb_batch_prepare(d, prec), "transform kernel attributes");
-        blocks[i] = lamb_batch_blocks(d, prec, part);
+        blocks[i] = lamb_batch_blocks(d, prec, part, xargs[i].stockham != 0);
         const int len = part == 1 ? d.NX2 : part == 3 ? 0 : d.NZ2;
-        groups[{prec, len}].push_back(i);
+        groups[std::make_tuple(prec, len, xargs[i].stockham)].push_back(i);
       }
       for (auto &g : groups)
-        for (auto &t : make_tables(xargs, blocks, g.second)) lamb.push_back({std::move(t), g.first.first, part});
+        for (auto &t : make_tables(xargs, blocks, g.second)) lamb.push_back({std::move(t), std::get<0>(g.first), part});
     }
     // nonlinear source
     std::vector<NLArgs> nargs;

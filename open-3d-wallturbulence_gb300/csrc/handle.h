@@ -168,6 +168,8 @@ struct owt_handle {
   void run_steps(int64_t n);
   int64_t per_step_launches = 0;
   bool force_dense = false;  // testing aid: always sweep the full band
+  bool fft_stockham = false; // FP32 transforms: shared-memory Stockham kernels instead of register ones
+  bool mean_split = true;    // mixed precision: the mean-flow terms of the Lamb vector in FP64 beside the transforms
   bool mean_smem = false;    // staged mean-mode solve in shared memory
   int modes_variant = 0;     // chosen by the autotuner
   int forced_variant = -1;   // testing aid: run this variant instead

@@ -182,6 +182,8 @@ void owt_handle::setup(const owt_params &prm) {
         const double b = sten.b(which, j, c);
         if (b != 0.0) {
           if (e >= 5) throw std::logic_error("stencil row wider than 5");
+          // the nonlinear-source kernel applies B1 with four taps per row
+          if (which == 0 && e >= 4) throw std::logic_error("first-derivative stencil row wider than 4");
           cols[(size_t)j * 5 + e] = c;
           vals[(size_t)j * 5 + e] = b;
           ++e;

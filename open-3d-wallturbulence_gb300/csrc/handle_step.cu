@@ -25,13 +25,14 @@ XformArgs owt_handle::xform_args() const {
   a.ring_mask = (1 << 1) | (1 << 4);
   a.fs = fs;
   a.step = d_step;
-  a.mean_split = precision == OWT_PREC_MIXED ? 1 : 0;
+  a.mean_split = (precision == OWT_PREC_MIXED && mean_split) ? 1 : 0;
   for (int f = 0; f < 3; ++f) a.lm[f] = lm + (size_t)f * fs;
   a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
   a.zbuf = zbuf; a.lbuf = lbuf;
   a.px = px; a.pz = pz;
   a.twx = twx[precision]; a.twz = twz[precision];
   a.inv_nx2 = 1.0 / (double)NX2; a.inv_nz2 = 1.0 / (double)NZ2;
+  a.stockham = fft_stockham ? 1 : 0;
   return a;
 }
 
@@ -42,6 +43,7 @@ NLArgs owt_handle::nl_args(bool record_mean) const {
   a.lx = lx; a.ly = ly; a.lz = lz;
   a.hv_ring = hv_ring; a.hg_ring = hg_ring;
   a.ab1 = b1.ab; a.piv1 = b1.piv; a.b1_col = b1_col; a.b1_val = b1_val;
+  a.fscr = bf;
   a.yscr = yscr;
   a.lx_mean = record_mean ? lxm_ring : nullptr;
   a.lz_mean = record_mean ? lzm_ring : nullptr;

@@ -16,17 +16,20 @@ template <> struct cpx_t<double> { using type = double2; };
 template <> struct cpx_t<float> { using type = float2; };
 template <typename T> using cpx = typename cpx_t<T>::type;
 
-template <typename T> __device__ __forceinline__ cpx<T> mk(T x, T y) { cpx<T> r; r.x = x; r.y = y; return r; }
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename T> __host__ __device__ __forceinline__ cpx<T> mk(T x, T y) { cpx<T> r; r.x = x; r.y = y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 // a * b
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
   C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
 // a * conj(b)
-template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
   C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
 }
+
+
+// Complex values between the FP64 state and the FP32 transforms.
 __device__ __forceinline__ double2 to_d(double2 a) { return a; }
 __device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
 template <typename T> __device__ __forceinline__ cpx<T> from_d(double2 a);
@@ -212,6 +215,28 @@ __device__ cpx<T> *fft_lines(cpx<T> *a, cpx<T> *b, int nlines, int lstride, cons
     cpx<T> *tmp = a; a = b; b = tmp;
   }
   return a;
+}
+
+// Point mm of the complex line whose backward FFT is a + i b, for the
+// spectra A, B (kx = 0 .. NXH-1) of two real lines: Hermitian extension in x
+// (slot i = u_i, slot NX2 - i = conj u_i, FFT.cpp:109-119), the imaginary
+// part of u_0 ignored (the real part of the reference's c2c output), slots
+// NXH .. NX2-NXH zero (padding).  MAYBE_NO_B: B may be null (b = 0).
+template <typename T, bool MAYBE_NO_B = false>
+__device__ __forceinline__ cpx<T> hermitian_pair(const cpx<T> *A, const cpx<T> *B, int mm, int NXH, int NX2) {
+  const cpx<T> zero = mk<T>((T)0, (T)0);
+  const bool hb = !MAYBE_NO_B || B != nullptr;
+  if (mm == 0) return mk<T>(A[0].x, hb ? B[0].x : (T)0);
+  if (mm < NXH) {
+    const cpx<T> x = A[mm], y = hb ? B[mm] : zero;
+    return mk<T>(x.x - y.y, x.y + y.x);
+  }
+  if (mm > NX2 - NXH) {
+    const int mp = NX2 - mm;
+    const cpx<T> x = A[mp], y = hb ? B[mp] : zero;
+    return mk<T>(x.x + y.y, y.x - x.y);
+  }
+  return zero;
 }
 
 // Value helpers so the band solves run on one real component (double) or a

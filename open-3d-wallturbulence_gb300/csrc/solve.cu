@@ -532,52 +532,55 @@ void launch_mean_batch(const BatchTable<MeanArgs> &t, bool smem, size_t smem_byt
 }
 
 // ---------------------------------------------------------------------------
-// nonlinear_source (src/solver.cpp:240-260), one thread per mode:
+// nonlinear_source (src/solver.cpp:240-260), one thread per real component of
+// a mode (lanes 2m, 2m+1 are Re, Im of mode m; A1 and B1 are real):
 //   Hg = i kz lx - i kx lz,   Hv = -k^2 ly - c11 A1^-1 B1 (i kx lx + i kz lz)
-// written to the level-0 slot; the thread of mode (0, 0) also records the
-// new mean Lamb vector (src/solver.cpp:296-302).
+// written to the level-0 slot.  Pass 1 forms this lane's component of
+// f = i kx lx + i kz lz once per row (scratch) and Hg; pass 2 applies B1 (at
+// most four taps per row, checked at setup) inside the right-hand side of the
+// A1 band solve and writes Hv from its output.  Component c of i z is
+// (2c - 1) times the other component of z.  The lane of component 0 of mode
+// (0, 0) also records the new mean Lamb vector (src/solver.cpp:296-302).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void nl_body(const NLArgs &a, const int m) {
+__device__ __forceinline__ void nl_body(const NLArgs &a, const int tid) {
+  const int m = tid >> 1, comp = tid & 1;
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
   const int k = m / a.NXH, i = m - k * a.NXH;
+  const double sgn = comp ? 1.0 : -1.0;
   const double kx = a.kx[i], kz = a.kz[k];
+  const double skx = sgn * kx, skz = sgn * kz;
   const double k2 = kx * kx + kz * kz;
   const int h = ring_head(*a.step);
   const size_t fs = (size_t)NY * M;
-  double2 *hv = a.hv_ring + (size_t)h * fs, *hg = a.hg_ring + (size_t)h * fs;
-  auto fval = [&](int j) -> double2 {
-    const double2 x = a.lx[(size_t)j * M + m], z = a.lz[(size_t)j * M + m];
-    return make_double2(-kx * x.y - kz * z.y, kx * x.x + kz * z.x);
-  };
-  // The solve asks for each right-hand side once, in increasing row order:
-  // row p's B1 (i kx lx + i kz lz) is formed there, and Hg of row p with it.
-  auto rhs = [&](int p) -> double2 {
-    double2 acc = make_double2(0.0, 0.0);
+  const double *lx = reinterpret_cast<const double *>(a.lx), *ly = reinterpret_cast<const double *>(a.ly);
+  const double *lz = reinterpret_cast<const double *>(a.lz);
+  double *hv = reinterpret_cast<double *>(a.hv_ring + (size_t)h * fs) + comp;
+  double *hg = reinterpret_cast<double *>(a.hg_ring + (size_t)h * fs) + comp;
+  double *f = reinterpret_cast<double *>(a.fscr) + comp;
+  double *y = reinterpret_cast<double *>(a.yscr) + comp;
+  auto E = [&](int j) { return 2 * ((size_t)j * M + m); };
+  const int oc = 1 - comp;
+  for (int j = 0; j < NY; ++j) {
+    const size_t e = E(j);
+    const double x = lx[e + oc], z = lz[e + oc];
+    f[e] = skx * x + skz * z;
+    hg[e] = skz * x - skx * z;
+  }
+  auto rhs = [&](int p) -> double {
+    double acc = 0.0;
 #pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      const double b = a.b1_val[p * 5 + e];
-      if (b != 0.0) {
-        const double2 f = fval(a.b1_col[p * 5 + e]);
-        acc.x += b * f.x;
-        acc.y += b * f.y;
-      }
-    }
-    const size_t at = (size_t)p * M + m;
-    const double2 x = a.lx[at], z = a.lz[at];
-    hg[at] = make_double2(-kz * x.y + kx * z.y, kz * x.x - kx * z.x);
+    for (int q = 0; q < 4; ++q) acc += a.b1_val[p * 5 + q] * f[E(a.b1_col[p * 5 + q])];
     return acc;
   };
-  auto ys = [&](int p, double2 y) { a.yscr[(size_t)p * M + m] = y; };
-  auto yl = [&](int p) -> double2 { return a.yscr[(size_t)p * M + m]; };
-  auto out = [&](int c, double2 d) {
-    const size_t at = (size_t)c * M + m;
-    const double2 ly = a.ly[at];
-    const double c11 = a.c11[c];
-    hv[at] = make_double2(-k2 * ly.x - c11 * d.x, -k2 * ly.y - c11 * d.y);
+  auto ys = [&](int p, double v) { y[E(p)] = v; };
+  auto yl = [&](int p) -> double { return y[E(p)]; };
+  auto out = [&](int c, double d) {
+    const size_t e = E(c);
+    hv[e] = -k2 * ly[e + comp] - a.c11[c] * d;
   };
   band_solve<2, 2>(a.ab1, a.piv1, NY, 1, 0, rhs, ys, yl, out);
-  if (m == 0 && a.lx_mean) {
+  if (m == 0 && comp == 0 && a.lx_mean) {
     for (int j = 0; j < NY; ++j) {
       a.lx_mean[(size_t)h * NY + j] = a.lx[(size_t)j * M];
       a.lz_mean[(size_t)h * NY + j] = a.lz[(size_t)j * M];
@@ -594,10 +597,10 @@ __global__ void __launch_bounds__(128) k_nl_batch(const __grid_constant__ BatchT
 }
 
 void launch_nl(const NLArgs &a, cudaStream_t st) {
-  const int bs = 128, gs = (a.M + bs - 1) / bs;
+  const int bs = 128, gs = (2 * a.M + bs - 1) / bs;
   k_nl<<<gs, bs, 0, st>>>(a);
 }
-int nl_batch_blocks(const NLArgs &a) { return (a.M + 127) / 128; }
+int nl_batch_blocks(const NLArgs &a) { return (2 * a.M + 127) / 128; }
 void launch_nl_batch(const BatchTable<NLArgs> &t, cudaStream_t st) { k_nl_batch<<<t.start[t.n], 128, 0, st>>>(t); }
 
 // ---------------------------------------------------------------------------

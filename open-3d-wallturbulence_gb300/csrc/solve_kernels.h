@@ -74,7 +74,7 @@ struct NLArgs {
   double2 *hv_ring, *hg_ring;
   const double *ab1; const uint8_t *piv1;
   const int *b1_col; const double *b1_val;
-  double2 *yscr;               // forward-sweep scratch [NY][M]
+  double2 *fscr, *yscr;        // B1 operand and forward-sweep scratch [NY][M] each
   double2 *lx_mean, *lz_mean;  // rings [3][NY], or null
   const long long *step;
 };
@@ -128,6 +128,7 @@ struct XformArgs {
   FftPlan px, pz;
   const void *twx, *twz;  // tables of exp(-2 pi i k/L) in T precision
   double inv_nx2, inv_nz2;
+  int stockham;  // FP32: 1 = the shared-memory Stockham kernels even where register ones exist
 };
 
 bool band_supported(int kl, int ku);
@@ -172,6 +173,19 @@ int launch_lamb(const XformArgs &a, int precision, cudaStream_t st);
 cudaError_t lamb_prepare(const XformDims &d);
 void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t st);
 size_t lamb_zbuf_bytes(const XformDims &d, int precision);
+// FP32 transform kernels with register-resident line transforms
+// (transforms_reg.cu) for one line length: ok = false when the length has no
+// two-pass factorisation there (the shared-memory Stockham kernels serve it).
+struct RegXformKernels {
+  bool ok = false;
+  void (*zback)(XformArgs) = nullptr, (*xlamb)(XformArgs) = nullptr, (*zfwd)(XformArgs) = nullptr;
+  void (*zback_b)(BatchTable<XformArgs>) = nullptr, (*xlamb_b)(BatchTable<XformArgs>) = nullptr,
+      (*zfwd_b)(BatchTable<XformArgs>) = nullptr;
+  int zthreads = 0, xthreads = 0, xlines = 0;  // xlines: (y, z) lines per x group
+  int xgrid = 0;  // the x pass is persistent: launch at most this many blocks (the resident ones)
+  size_t zsmem = 0, xsmem = 0;
+};
+RegXformKernels reg_xform_kernels(int L);
 // Stand-alone FP64 dealiased transforms of one field (zbuf / lbuf field 0 in
 // between): a.in[0] -> phys [y][z][x], and phys -> a.out[0].
 cudaError_t phys_prepare(const XformDims &d);
@@ -220,7 +234,7 @@ void launch_nl_batch(const BatchTable<NLArgs> &t, cudaStream_t st);
 // Transforms: part 0 z backward, 1 x pass, 2 z forward, 3 mean-flow terms
 // (mixed precision).  The channels of a table share the precision, NZ2 (parts
 // 0, 2) or NX2 (part 1).
-int lamb_batch_blocks(const XformDims &d, int precision, int part);
+int lamb_batch_blocks(const XformDims &d, int precision, int part, bool stockham);
 cudaError_t lamb_batch_prepare(const XformDims &d, int precision);
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st);
 

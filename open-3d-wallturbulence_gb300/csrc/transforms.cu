@@ -74,28 +74,6 @@ __device__ __forceinline__ void zback_body(const XformArgs &a, const int bx, con
   }
 }
 
-// Point mm of the complex line whose backward FFT is a + i b, for the
-// spectra A, B (kx = 0 .. NXH-1) of two real lines: Hermitian extension in x
-// (slot i = u_i, slot NX2 - i = conj u_i, FFT.cpp:109-119), the imaginary
-// part of u_0 ignored (the real part of the reference's c2c output), slots
-// NXH .. NX2-NXH zero (padding).  MAYBE_NO_B: B may be null (b = 0).
-template <typename T, bool MAYBE_NO_B = false>
-__device__ __forceinline__ cpx<T> hermitian_pair(const cpx<T> *A, const cpx<T> *B, int mm, int NXH, int NX2) {
-  const cpx<T> zero = mk<T>((T)0, (T)0);
-  const bool hb = !MAYBE_NO_B || B != nullptr;
-  if (mm == 0) return mk<T>(A[0].x, hb ? B[0].x : (T)0);
-  if (mm < NXH) {
-    const cpx<T> x = A[mm], y = hb ? B[mm] : zero;
-    return mk<T>(x.x - y.y, x.y + y.x);
-  }
-  if (mm > NX2 - NXH) {
-    const int mp = NX2 - mm;
-    const cpx<T> x = A[mp], y = hb ? B[mp] : zero;
-    return mk<T>(x.x + y.y, y.x - x.y);
-  }
-  return zero;
-}
-
 template <typename T, int P, bool R5>
 __device__ __forceinline__ void xlamb_body(const XformArgs &a, const int bx) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -191,11 +169,13 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
       const int slot = kz < d.NZH ? kz : kz + d.NZH;
       const double2 v = to_d(r[c * ls + sw<T>(slot)]);
       const size_t at = (size_t)kz * d.NXH + i0 + c;
-      double2 o = make_double2(v.x * sc, v.y * sc);
+      // explicit roundings: the batched and the one-channel kernels must
+      // give the same bits whatever each compilation contracts
+      double2 o = make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
       if (kSplit && lm) {
         const double2 l = lm[at];
-        o.x += l.x;
-        o.y += l.y;
+        o.x = __dadd_rn(o.x, l.x);
+        o.y = __dadd_rn(o.y, l.y);
       }
       dst[at] = o;
     }
@@ -404,18 +384,29 @@ static int x_lines(const XformDims &d) {
 
 // The instances a channel's transforms use: by precision, x lines per block
 // and radix-5 stages of the z and x lines.
+// FP32 lines with a two-pass factorisation (transforms_reg.cu) use the
+// register-transform kernels unless `stockham` is set; they keep TX = 12
+// columns per z block, and P (y, z) lines per x block of their own.
 template <typename T>
 struct XformKernels {
   int P;
   void (*zback)(XformArgs), (*xlamb)(XformArgs), (*zfwd)(XformArgs);
   void (*zback_b)(BatchTable<XformArgs>), (*xlamb_b)(BatchTable<XformArgs>), (*zfwd_b)(BatchTable<XformArgs>);
+  int zthreads, xthreads;
+  size_t zsmem, xsmem;
+  int xgrid;  // x-pass blocks at most (0: one block per group of P lines)
 };
 template <typename T>
-static XformKernels<T> kernels(const XformDims &d) {
+static XformKernels<T> kernels(const XformDims &d, bool stockham = false) {
   constexpr int PP = XCfg<T>::P;
   const bool z5 = d.NZ2 % 5 == 0, x5 = d.NX2 % 5 == 0;
   XformKernels<T> k;
   k.P = x_lines<T>(d);
+  k.zthreads = d.NZ2;
+  k.xthreads = d.NX2;
+  k.zsmem = smem_z<T>(d);
+  k.xsmem = smem_x<T>(d, k.P);
+  k.xgrid = 0;
   k.zback = z5 ? k_zback<T, true> : k_zback<T, false>;
   k.zfwd = z5 ? k_zfwd<T, true> : k_zfwd<T, false>;
   k.zback_b = z5 ? k_zback_batch<T, true> : k_zback_batch<T, false>;
@@ -427,6 +418,22 @@ static XformKernels<T> kernels(const XformDims &d) {
     k.xlamb = x5 ? k_xlamb<T, 2, true> : k_xlamb<T, 2, false>;
     k.xlamb_b = x5 ? k_xlamb_batch<T, 2, true> : k_xlamb_batch<T, 2, false>;
   }
+  if (sizeof(T) == sizeof(float) && !stockham) {
+    static_assert(XCfg<float>::TX == 12, "register z kernels assume the FP32 z block shape");
+    const RegXformKernels rz = reg_xform_kernels(d.NZ2), rx = reg_xform_kernels(d.NX2);
+    if (rz.ok) {
+      k.zback = rz.zback; k.zfwd = rz.zfwd; k.zback_b = rz.zback_b; k.zfwd_b = rz.zfwd_b;
+      k.zthreads = rz.zthreads;
+      k.zsmem = rz.zsmem;
+    }
+    if (rx.ok) {
+      k.xlamb = rx.xlamb; k.xlamb_b = rx.xlamb_b;
+      k.xthreads = rx.xthreads;
+      k.xsmem = rx.xsmem;
+      k.P = rx.xlines;
+      k.xgrid = rx.xgrid;
+    }
+  }
   return k;
 }
 
@@ -435,16 +442,17 @@ static XformKernels<T> kernels(const XformDims &d) {
 template <typename T>
 static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   const XformDims &d = a.d;
-  const XformKernels<T> k = kernels<T>(d);
+  const XformKernels<T> k = kernels<T>(d, a.stockham != 0);
   constexpr int TX = XCfg<T>::TX;
-  const size_t sz = smem_z<T>(d);
   if (part == 0) {
-    k.zback<<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), d.NZ2, sz, st>>>(a);
+    k.zback<<<dim3((d.NXH + TX - 1) / TX, d.NY, 6), k.zthreads, k.zsmem, st>>>(a);
   } else if (part == 1) {
     const size_t nl = (size_t)d.NY * d.NZ2;
-    k.xlamb<<<(unsigned)((nl + k.P - 1) / k.P), d.NX2, smem_x<T>(d, k.P), st>>>(a);
+    size_t grid = (nl + k.P - 1) / k.P;
+    if (k.xgrid > 0 && grid > (size_t)k.xgrid) grid = k.xgrid;
+    k.xlamb<<<(unsigned)grid, k.xthreads, k.xsmem, st>>>(a);
   } else if (part == 2) {
-    k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), d.NZ2, sz, st>>>(a);
+    k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), k.zthreads, k.zsmem, st>>>(a);
   } else if (a.mean_split) {
     launch_mean_lamb(a, st);
   }
@@ -463,14 +471,16 @@ static int lamb_t(const XformArgs &a, cudaStream_t st) {
 // shared memory they need, before any launch or graph capture.
 template <typename T>
 static cudaError_t prepare_t(const XformDims &d) {
-  const XformKernels<T> k = kernels<T>(d);
-  const size_t sz = smem_z<T>(d), sx = smem_x<T>(d, k.P);
-  cudaError_t e = raise_smem_limit(k.zback, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k.zfwd, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k.xlamb, sx);
-  if (e == cudaSuccess) e = raise_smem_limit(k.zback_b, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k.zfwd_b, sz);
-  if (e == cudaSuccess) e = raise_smem_limit(k.xlamb_b, sx);
+  cudaError_t e = cudaSuccess;
+  for (int stockham = 0; stockham < 2 && e == cudaSuccess; ++stockham) {
+    const XformKernels<T> k = kernels<T>(d, stockham != 0);
+    e = raise_smem_limit(k.zback, k.zsmem);
+    if (e == cudaSuccess) e = raise_smem_limit(k.zfwd, k.zsmem);
+    if (e == cudaSuccess) e = raise_smem_limit(k.xlamb, k.xsmem);
+    if (e == cudaSuccess) e = raise_smem_limit(k.zback_b, k.zsmem);
+    if (e == cudaSuccess) e = raise_smem_limit(k.zfwd_b, k.zsmem);
+    if (e == cudaSuccess) e = raise_smem_limit(k.xlamb_b, k.xsmem);
+  }
   return e;
 }
 
@@ -491,18 +501,18 @@ void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t 
 // Blocks of one channel in part 0 (z backward), 1 (x pass), 2 (z forward) or
 // 3 (mean-flow terms); the grids of the one-channel launches, flattened.
 template <typename T>
-static int lamb_blocks_t(const XformDims &d, int part) {
+static int lamb_blocks_t(const XformDims &d, int part, bool stockham) {
   const int gx = (d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX;
   if (part == 0) return gx * d.NY * 6;
   if (part == 2) return gx * d.NY * 3;
   if (part == 1) {
-    const int P = x_lines<T>(d);
+    const int P = kernels<T>(d, stockham).P;
     return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
   }
   return ((d.NZ * d.NXH + 255) / 256) * d.NY;
 }
-int lamb_batch_blocks(const XformDims &d, int precision, int part) {
-  return precision == 0 ? lamb_blocks_t<double>(d, part) : lamb_blocks_t<float>(d, part);
+int lamb_batch_blocks(const XformDims &d, int precision, int part, bool stockham) {
+  return precision == 0 ? lamb_blocks_t<double>(d, part, stockham) : lamb_blocks_t<float>(d, part, stockham);
 }
 
 cudaError_t lamb_batch_prepare(const XformDims &d, int precision) {
@@ -512,11 +522,12 @@ cudaError_t lamb_batch_prepare(const XformDims &d, int precision) {
 template <typename T>
 static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t st) {
   const XformDims &d = t.a[0].d;
-  const XformKernels<T> k = kernels<T>(d);
+  const XformKernels<T> k = kernels<T>(d, t.a[0].stockham != 0);
   const unsigned blocks = (unsigned)t.start[t.n];
-  if (part == 0) k.zback_b<<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
-  else if (part == 1) k.xlamb_b<<<blocks, d.NX2, smem_x<T>(d, k.P), st>>>(t);
-  else if (part == 2) k.zfwd_b<<<blocks, d.NZ2, smem_z<T>(d), st>>>(t);
+  if (part == 0) k.zback_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
+  else if (part == 1) k.xlamb_b<<<k.xgrid > 0 && blocks > (unsigned)k.xgrid ? (unsigned)k.xgrid : blocks, k.xthreads,
+                                  k.xsmem, st>>>(t);
+  else if (part == 2) k.zfwd_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
   else k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
 }
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {

@@ -199,6 +199,17 @@ class GpuSolver:
     def force_dense_bands(self, on=True):
         self._chk(self.L.owt_set_option(self.h, 1, 1 if on else 0))
 
+    def use_stockham_fft(self, on=True):
+        """FP32 transforms through the shared-memory Stockham kernels instead of
+        the register-transform ones (OWT_OPT_FFT_STOCKHAM), for comparisons."""
+        self._chk(self.L.owt_set_option(self.h, 3, 1 if on else 0))
+
+    def use_mean_split(self, on=True):
+        """Mixed precision: FP64 mean-flow terms of the Lamb vector beside the
+        FP32 transforms (the default), or the whole fields through FP32
+        (OWT_OPT_MEAN_SPLIT)."""
+        self._chk(self.L.owt_set_option(self.h, 4, 1 if on else 0))
+
     def force_modes_variant(self, v):
         """Run mode-kernel variant v (-1: the autotuned one)."""
         self._chk(self.L.owt_set_option(self.h, 2, int(v)))
