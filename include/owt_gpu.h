@@ -131,6 +131,28 @@ int owt_init_seeded(owt_handle *h, uint64_t seed, double rms);
  * synchronizing call. */
 int owt_time_integration(owt_handle *h, int64_t nsteps);
 
+/* time_Integration (src/solver.cpp:541-627) on a state the caller holds on
+ * the host, as the reference keeps it in its globals: uploads the history
+ * fields, runs one step, and returns the new v and omega_y and the friction
+ * histories.  The handle's device state becomes that of the step.
+ *  - hist: 12 arrays [z][x][y] complex128, in the order vely_0, vely_1,
+ *    vely_2, vory_0, vory_1, vory_2, Hv_0, Hv_1, Hv_2, Hg_0, Hg_1, Hg_2
+ *    (src/setup.hpp:64-67);
+ *  - means: the 12 mean-mode history vectors in enum owt_mean order, NY
+ *    complex128 each, consecutive;
+ *  - fric: fx_fric_0..2, fz_fric_0..2;
+ *  - vely, vory: out, the step's new v and omega_y, [z][x][y] complex128;
+ *    fric_out: out, the friction histories after the step.
+ * Copies overlap the device work: the twelve host-to-device copies run back
+ * to back into staging buffers of their own (the first call allocates them:
+ * 12 + 2 fields of device memory, kept by the handle), each field's layout
+ * transpose follows its copy, the DY2 v history of the v levels is
+ * re-derived while the other fields arrive, and v and omega_y travel back
+ * while the step's transforms run.  Pinned host arrays give the full copy
+ * rate.  Synchronous: when it returns, the outputs are written. */
+int owt_time_integration_host(owt_handle *h, const double *const *hist, const double *means, const double *fric,
+                              double *vely, double *vory, double *fric_out);
+
 /* Run one reference routine on the current state (enum owt_routine). */
 int owt_call(owt_handle *h, int routine);
 

@@ -334,6 +334,16 @@ int owt_dy_apply(owt_handle *h, int order, const double *in, double *out) {
   });
 }
 
+int owt_time_integration_host(owt_handle *h, const double *const *hist, const double *means, const double *fric,
+                              double *vely, double *vory, double *fric_out) {
+  return guard(h, [&] {
+    if (!hist || !means || !fric || !vely || !vory || !fric_out) throw OwtError(OWT_ERR_INVALID, "null buffer");
+    for (int i = 0; i < 12; ++i)
+      if (!hist[i]) throw OwtError(OWT_ERR_INVALID, "null history field");
+    h->step_host(hist, means, fric, vely, vory, fric_out);
+  });
+}
+
 int owt_fourier2physical(owt_handle *h, const double *spec, double *phys) {
   return guard(h, [&] {
     if (!spec || !phys) throw OwtError(OWT_ERR_INVALID, "null buffer");

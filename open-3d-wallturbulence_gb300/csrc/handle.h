@@ -158,7 +158,9 @@ struct owt_handle {
   // launch sequence (or its CUDA graph) serves every step.
   // The mean mode runs on a second stream beside the mode kernel (they touch
   // disjoint data); both read the counter before it advances.
-  void enqueue_step();
+  // after_modes: recorded on the stream right after the mode kernel (the new
+  // v and omega_y are final from then on), when given
+  void enqueue_step(cudaEvent_t after_modes = nullptr);
   void stage_modes();
   bool modes_sparse() const { return sparse_v && !force_dense; }
   owt::ModeArgs mode_args() const;
@@ -188,7 +190,7 @@ struct owt_handle {
   void drop_graph();
 
   // DY2 v for history levels whose v was replaced from the host (one launch).
-  void recompute_dirty_q();
+  void recompute_dirty_q(cudaStream_t on = nullptr);  // on: another stream than the handle's
 
   void copy_ring(double2 *ring, size_t n, int from, int to);
   // column of mode 0 of a device-layout field -> contiguous NY vector
@@ -215,6 +217,21 @@ struct owt_handle {
   // spectral [z][x][y] complex128 <-> physical [z][x][y] doubles on the 3/2
   // grid (src/FFT.cpp:49-194); temporary device buffers for the physical field.
   void fourier2physical(const double *spec, double *phys);
+  // One step on a state held by the caller on the host (owt_time_integration_host):
+  // 12 history fields, 12 mean vectors, 6 friction values in; new v, omega_y
+  // and the friction histories out; copies overlapped with the device work.
+  struct HostStep {
+    bool ready = false;
+    // H2D copies; layout transposes (high priority); DY2 v; D2H transposes
+    // and copies (high priority)
+    cudaStream_t up = nullptr, tx = nullptr, aux = nullptr, down = nullptr;
+    double2 *stage[12] = {}, *dstage[2] = {nullptr, nullptr};
+    cudaEvent_t landed[12] = {}, v_done = nullptr, q_done = nullptr, up_done = nullptr, tx_done = nullptr,
+                after_modes = nullptr, down_done = nullptr;
+  } hs;
+  void host_step_prepare();
+  void step_host(const double *const *hist, const double *means, const double *fric, double *v_out, double *g_out,
+                 double *fric_out);
   void physical2fourier(const double *phys, double *spec);
   double2 *mean_ptr(int which);
   // ---- wall-drag adjoint -------------------------------------------------------

@@ -17,6 +17,14 @@ owt_handle::~owt_handle() {
   for (void *q : owned) cudaFree(q);
   for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
     if (e) cudaEventDestroy(e);
+  if (hs.ready) {
+    for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamSynchronize(q);
+    for (cudaEvent_t e : hs.landed)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {hs.v_done, hs.q_done, hs.up_done, hs.tx_done, hs.after_modes, hs.down_done})
+      if (e) cudaEventDestroy(e);
+    for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamDestroy(q);
+  }
   if (st2) cudaStreamDestroy(st2);
   if (st) cudaStreamDestroy(st);
 }

@@ -56,12 +56,13 @@ NLArgs owt_handle::nl_args(bool record_mean) const {
 // launch sequence (or its CUDA graph) serves every step.
 // The mean mode runs on a second stream beside the mode kernel (they touch
 // disjoint data); both read the counter before it advances.
-void owt_handle::enqueue_step() {
+void owt_handle::enqueue_step(cudaEvent_t after_modes) {
   ck(cudaEventRecord(ev_fork, st), "fork");
   ck(cudaStreamWaitEvent(st2, ev_fork, 0), "fork wait");
   stage_mean(true, st2);
   ck(cudaEventRecord(ev_join, st2), "join");
   stage_modes();
+  if (after_modes) ck(cudaEventRecord(after_modes, st), "after modes");
   ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launch_advance(d_step, st);
   const XformArgs xa = xform_args();
@@ -220,7 +221,7 @@ void owt_handle::autotune_modes() {
 }
 
 // DY2 v for history levels whose v was replaced from the host (one launch).
-void owt_handle::recompute_dirty_q() {
+void owt_handle::recompute_dirty_q(cudaStream_t on) {
   DY2Args a{};
   a.NY = NY; a.M = M;
   a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
@@ -236,7 +237,7 @@ void owt_handle::recompute_dirty_q() {
     q_dirty[sl] = false;
   }
   if (!a.nf) return;
-  launch_dy2(a, st);
+  launch_dy2(a, on ? on : st);
   ++launches;
 }
 
@@ -437,4 +438,95 @@ void owt_handle::physical2fourier(const double *phys, double *spec) {
     throw;
   }
   for (void *q : tmp) cudaFree(q);
+}
+
+// ---- one step on a host-held state ---------------------------------------------
+void owt_handle::host_step_prepare() {
+  if (hs.ready) return;
+  int lo = 0, hi = 0;
+  ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+  ck(cudaStreamCreateWithFlags(&hs.up, cudaStreamNonBlocking), "stream");
+  ck(cudaStreamCreateWithFlags(&hs.aux, cudaStreamNonBlocking), "stream");
+  ck(cudaStreamCreateWithPriority(&hs.tx, cudaStreamNonBlocking, hi), "stream");
+  ck(cudaStreamCreateWithPriority(&hs.down, cudaStreamNonBlocking, hi), "stream");
+  for (int i = 0; i < 12; ++i) {
+    hs.stage[i] = dalloc<double2>(fs, owned);
+    ck(cudaEventCreateWithFlags(&hs.landed[i], cudaEventDisableTiming), "event");
+  }
+  for (int b = 0; b < 2; ++b) hs.dstage[b] = dalloc<double2>(fs, owned);
+  for (cudaEvent_t *e : {&hs.v_done, &hs.q_done, &hs.up_done, &hs.tx_done, &hs.after_modes, &hs.down_done})
+    ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
+  hs.ready = true;
+}
+
+// Uploads: every field has a staging buffer of its own, so the twelve
+// host-to-device copies run back to back on the copy stream; each field's
+// layout transpose into its ring slot follows its copy on a high-priority
+// stream (whose blocks the scheduler places ahead of those of long kernels).
+// The DY2 v history of the three uploaded v levels is re-derived on a third
+// stream while the other nine fields are still arriving.  Downloads: the new
+// v and omega_y are final after the mode kernel, so their transposes (high
+// priority) and copies run beside the transforms of the same step.
+void owt_handle::step_host(const double *const *hist, const double *means, const double *fric, double *v_out,
+                           double *g_out, double *fric_out) {
+  host_step_prepare();
+  ensure_tuned();
+  ck(cudaStreamSynchronize(st), "host step");
+  double2 *rings[4] = {v_ring, g_ring, hv_ring, hg_ring};
+  for (int i = 0; i < 12; ++i) {
+    ck(cudaMemcpyAsync(hs.stage[i], hist[i], fs * sizeof(double2), cudaMemcpyHostToDevice, hs.up), "H2D");
+    ck(cudaEventRecord(hs.landed[i], hs.up), "landed");
+  }
+  for (int w = 0; w < OWT_NUM_MEANS; ++w)
+    ck(cudaMemcpyAsync(mean_ptr(w), means + 2 * (size_t)w * NY, NY * sizeof(double2), cudaMemcpyHostToDevice, hs.up),
+       "H2D");
+  ck(cudaEventRecord(hs.up_done, hs.up), "uploads done");
+  for (int i = 0; i < 12; ++i) {
+    ck(cudaStreamWaitEvent(hs.tx, hs.landed[i], 0), "landed wait");
+    launch_transpose(hs.stage[i], ring_level(rings[i / 3], i % 3), M, NY, hs.tx);  // [M][NY] -> [NY][M]
+    ++launches;
+    if (i == 2) {  // the three v levels are in place: DY2 v on the side
+      ck(cudaEventRecord(hs.v_done, hs.tx), "v done");
+      ck(cudaStreamWaitEvent(hs.aux, hs.v_done, 0), "v wait");
+      q_dirty[0] = q_dirty[1] = q_dirty[2] = true;
+      recompute_dirty_q(hs.aux);
+      ck(cudaEventRecord(hs.q_done, hs.aux), "q done");
+    }
+  }
+  ck(cudaEventRecord(hs.tx_done, hs.tx), "transposes done");
+  {
+    double fx[3], fz[3];
+    for (int l = 0; l < 3; ++l) {
+      fx[slot(l)] = fric[l];
+      fz[slot(l)] = fric[3 + l];
+    }
+    ck(cudaMemcpyAsync(fx_ring, fx, sizeof(fx), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(fz_ring, fz, sizeof(fz), cudaMemcpyHostToDevice, st), "H2D");
+  }
+  for (cudaEvent_t e : {hs.up_done, hs.tx_done, hs.q_done}) ck(cudaStreamWaitEvent(st, e, 0), "uploads wait");
+  ++state_version;
+  initialized = true;
+  // the new v, omega_y land in the slot that becomes level 0 after the step
+  const int hn = (head() + 2) % 3;
+  enqueue_step(hs.after_modes);
+  ++steps;
+  ck(cudaStreamWaitEvent(hs.down, hs.after_modes, 0), "modes wait");
+  double *outs[2] = {v_out, g_out};
+  double2 *src[2] = {v_ring + (size_t)hn * fs, g_ring + (size_t)hn * fs};
+  for (int b = 0; b < 2; ++b) {
+    launch_transpose(src[b], hs.dstage[b], NY, M, hs.down);  // [NY][M] -> [M][NY]
+    ++launches;
+    ck(cudaMemcpyAsync(outs[b], hs.dstage[b], fs * sizeof(double2), cudaMemcpyDeviceToHost, hs.down), "D2H");
+  }
+  ck(cudaEventRecord(hs.down_done, hs.down), "downloads done");
+  ck(cudaStreamWaitEvent(st, hs.down_done, 0), "downloads wait");
+  check_launch("host step");
+  double fx[3], fz[3];
+  ck(cudaMemcpyAsync(fx, fx_ring, sizeof(fx), cudaMemcpyDeviceToHost, st), "D2H");
+  ck(cudaMemcpyAsync(fz, fz_ring, sizeof(fz), cudaMemcpyDeviceToHost, st), "D2H");
+  sync_and_check();
+  for (int l = 0; l < 3; ++l) {
+    fric_out[l] = fx[slot(l)];
+    fric_out[3 + l] = fz[slot(l)];
+  }
 }

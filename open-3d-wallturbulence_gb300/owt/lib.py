@@ -73,6 +73,7 @@ def load(path=LIB):
         "owt_get_grid": ([_h, _dp], C.c_int),
         "owt_dy_apply": ([_h, C.c_int, _dp, _dp], C.c_int),
         "owt_fourier2physical": ([_h, _dp, _dp], C.c_int),
+        "owt_time_integration_host": ([_h, C.POINTER(_dp), _dp, _dp, _dp, _dp, _dp], C.c_int),
         "owt_physical2fourier": ([_h, _dp, _dp], C.c_int),
         "owt_enqueue_stage": ([_h, C.c_int], C.c_int),
         "owt_set_option": ([_h, C.c_int, C.c_int64], C.c_int),

@@ -132,6 +132,30 @@ class GpuSolver:
         self._chk(self.L.owt_dy_apply(self.h, int(order), _L.dptr(a.view(np.float64)), _L.dptr(out.view(np.float64))))
         return out
 
+    HISTORY = ("vely_0", "vely_1", "vely_2", "vory_0", "vory_1", "vory_2",
+               "Hv_0", "Hv_1", "Hv_2", "Hg_0", "Hg_1", "Hg_2")
+
+    def time_Integration_host(self, hist, means, fric, vely_out=None, vory_out=None):
+        """One step on a host-held state (owt_time_integration_host): `hist` the 12
+        history fields in HISTORY order ([z][x][y] complex128), `means` the 12
+        mean vectors as a (12, NY) complex128 array in the library's order,
+        `fric` the six friction values.  Returns (vely, vory, friction)."""
+        arrs = [self._c(a) for a in hist]
+        if len(arrs) != 12:
+            raise ValueError("12 history fields expected")
+        m = np.ascontiguousarray(means, dtype=np.complex128)
+        if m.shape != (12, self.params.NY):
+            raise ValueError(f"means must have shape (12, {self.params.NY})")
+        f = np.ascontiguousarray(fric, dtype=np.float64)
+        vo = np.empty(self.shape, np.complex128) if vely_out is None else vely_out
+        go = np.empty(self.shape, np.complex128) if vory_out is None else vory_out
+        fo = np.empty(6)
+        ptrs = (_L._dp * 12)(*[_L.dptr(a.view(np.float64)) for a in arrs])
+        self._chk(self.L.owt_time_integration_host(self.h, ptrs, _L.dptr(m.view(np.float64)), _L.dptr(f),
+                                                   _L.dptr(vo.view(np.float64)), _L.dptr(go.view(np.float64)),
+                                                   _L.dptr(fo)))
+        return vo, go, fo
+
     @property
     def physical_shape(self):
         p = self.params

@@ -183,3 +183,48 @@ def test_state_keep_and_restore_on_device(gpu_lib, run):
     np.testing.assert_array_equal(s.get("Hg"), first[1])
     np.testing.assert_array_equal(s.friction(), first[2])
     assert s.step == first[3]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_host_state_step_equals_device_step(gpu_lib, precision):
+    """owt_time_integration_host (one step on a host-held state, copies
+    overlapped with the device work) gives the bits of uploading the same
+    state with the set-field calls and stepping, whatever the receiving
+    handle's own ring position: the returned v, omega_y and friction, and the
+    handle's state afterwards, on two calls in a row.  Both re-derive the
+    DY2 v history of the uploaded v levels, which an uninterrupted run
+    carries from its own solves, so against the uninterrupted step they
+    agree to the one-step bound (1e-10)."""
+    from owt.ic import seeded_velocity
+    from owt.params import CaseParams
+    from owt.solver import GpuSolver
+    p = CaseParams(dt=0.002, dkx=1.0, dkz=2.0, NX=32, NY=33, NZ=24, alpha_mesh=2.2, nu=1e-4)
+    means_names = ("lmbx_mean_0", "lmbx_mean_1", "lmbx_mean_2", "lmbz_mean_0", "lmbz_mean_1", "lmbz_mean_2",
+                   "velx_mean_0", "velx_mean_1", "velx_mean_2", "velz_mean_0", "velz_mean_1", "velz_mean_2")
+    a = GpuSolver(p, precision=precision)
+    a.init_fields(*seeded_velocity(p, seed=3))
+    a.time_Integration(2)
+    hist = [a.get(n) for n in GpuSolver.HISTORY]
+    means = np.stack([a.get_cvec(n) for n in means_names])
+    fric = a.friction()
+    c = GpuSolver(p, precision=precision)
+    c.init_fields(*seeded_velocity(p, seed=9))
+    for n, x in zip(GpuSolver.HISTORY, hist):
+        c.set(n, x)
+    for n, x in zip(means_names, means):
+        c.set_cvec(n, x)
+    c.set_friction(fric)
+    c.time_Integration(1)
+    a.time_Integration(1)
+    b = GpuSolver(p, precision=precision)
+    b.init_fields(*seeded_velocity(p, seed=9))
+    b.time_Integration(1)  # a different ring position than c's
+    for rep in range(2):
+        v, g, f = b.time_Integration_host(hist, means, fric)
+        np.testing.assert_array_equal(v, c.get("vely"))
+        np.testing.assert_array_equal(g, c.get("vory"))
+        np.testing.assert_array_equal(f, c.friction())
+        for n in ("velx", "vorz", "lmbx", "lmbz", "Hv", "Hg", "vely_1", "Hv_2"):
+            np.testing.assert_array_equal(b.get(n), c.get(n))
+        for x, y in ((v, a.get("vely")), (g, a.get("vory"))):
+            assert np.abs(x - y).max() <= 1e-10 * np.abs(y).max()
