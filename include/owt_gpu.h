@@ -147,9 +147,11 @@ int owt_time_integration(owt_handle *h, int64_t nsteps);
  * to back into staging buffers of their own (the first call allocates them:
  * 12 + 2 fields of device memory, kept by the handle), each field's layout
  * transpose follows its copy, the DY2 v history of the v levels is
- * re-derived while the other fields arrive, and v and omega_y travel back
- * while the step's transforms run.  Pinned host arrays give the full copy
- * rate.  Synchronous: when it returns, the outputs are written. */
+ * re-derived while the other fields arrive, with a quad-mapping mode kernel
+ * the copies are pipelined with it over chunks of Fourier modes
+ * (OWT_OPT_HOST_CHUNKS), and v and omega_y travel back while the step's
+ * transforms run.  Pinned host arrays give the full copy rate.
+ * Synchronous: when it returns, the outputs are written. */
 int owt_time_integration_host(owt_handle *h, const double *const *hist, const double *means, const double *fric,
                               double *vely, double *vory, double *fric_out);
 
@@ -267,6 +269,9 @@ int owt_state_restore(owt_handle *h);
  *   transforms carry the fluctuations and the mean-flow terms of the Lamb
  *   vector (mean velocity x fluctuating vorticity and back) are formed in FP64
  *   spectrally beside them; 0 = the FP32 transforms carry the whole fields.
+ * OWT_OPT_HOST_CHUNKS: owt_time_integration_host pipelines its uploads with
+ *   the mode kernel over this many chunks of Fourier modes (1 .. 8; 0 = the
+ *   default, 2) when the mode kernel in use maps threads by quads.
  * OWT_INFO_SPARSE_SOLVE: 1 if the interior-sparse v-system solve is active.
  * OWT_INFO_PATTERN_VIOLATIONS: modes whose factors fell outside the sparse
  *   pattern at setup (any such mode selects the full-band solve).
@@ -280,6 +285,7 @@ int owt_state_restore(owt_handle *h);
 #define OWT_OPT_MODES_VARIANT 2
 #define OWT_OPT_FFT_STOCKHAM 3
 #define OWT_OPT_MEAN_SPLIT 4
+#define OWT_OPT_HOST_CHUNKS 5
 #define OWT_INFO_SPARSE_SOLVE 1
 #define OWT_INFO_PATTERN_VIOLATIONS 2
 #define OWT_INFO_DEVICE_BYTES 3

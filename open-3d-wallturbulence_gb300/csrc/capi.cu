@@ -241,6 +241,9 @@ int owt_set_option(owt_handle *h, int option, int64_t value) {
       h->fft_stockham = value != 0;
     } else if (option == OWT_OPT_MEAN_SPLIT) {
       h->mean_split = value != 0;
+    } else if (option == OWT_OPT_HOST_CHUNKS) {
+      if (value < 0 || value > 8) throw OwtError(OWT_ERR_INVALID, "host-step chunks must be within [0, 8]");
+      h->host_chunks = (int)value;
     } else if (option == OWT_OPT_MODES_VARIANT) {
       if (value < -1 || value >= modes_variant_count()) throw OwtError(OWT_ERR_INVALID, "no such variant");
       h->forced_variant = (int)value;

@@ -161,6 +161,8 @@ struct owt_handle {
   // after_modes: recorded on the stream right after the mode kernel (the new
   // v and omega_y are final from then on), when given
   void enqueue_step(cudaEvent_t after_modes = nullptr);
+  void step_begin();   // the mean mode forked beside the mode kernel
+  void step_finish();  // join, counter, Lamb vector, nonlinear source
   void stage_modes();
   bool modes_sparse() const { return sparse_v && !force_dense; }
   owt::ModeArgs mode_args() const;
@@ -172,6 +174,7 @@ struct owt_handle {
   bool force_dense = false;  // testing aid: always sweep the full band
   bool fft_stockham = false; // FP32 transforms: shared-memory Stockham kernels instead of register ones
   bool mean_split = true;    // mixed precision: the mean-flow terms of the Lamb vector in FP64 beside the transforms
+  int host_chunks = 0;       // owt_time_integration_host: chunks of modes (0: the default)
   bool mean_smem = false;    // staged mean-mode solve in shared memory
   int modes_variant = 0;     // chosen by the autotuner
   int forced_variant = -1;   // testing aid: run this variant instead
@@ -225,9 +228,14 @@ struct owt_handle {
     // H2D copies; layout transposes (high priority); DY2 v; D2H transposes
     // and copies (high priority)
     cudaStream_t up = nullptr, tx = nullptr, aux = nullptr, down = nullptr;
+    // chunks of Fourier modes the uploads and the mode kernel pipeline over:
+    // at most kChunks, kDefaultChunks unless set (measured at 384x257x384:
+    // 88.5 ms a call with one chunk, 82.7 with two, 85.8 with four, 110 with
+    // eight, whose DY2 v re-derivations compete with the mode kernel)
+    static constexpr int kChunks = 8, kDefaultChunks = 2;
     double2 *stage[12] = {}, *dstage[2] = {nullptr, nullptr};
-    cudaEvent_t landed[12] = {}, v_done = nullptr, q_done = nullptr, up_done = nullptr, tx_done = nullptr,
-                after_modes = nullptr, down_done = nullptr;
+    cudaEvent_t landed[kChunks] = {}, v_done[kChunks] = {}, q_done[kChunks] = {}, tx_done[kChunks] = {};
+    cudaEvent_t up_done = nullptr, after_modes = nullptr, down_done = nullptr;
   } hs;
   void host_step_prepare();
   void step_host(const double *const *hist, const double *means, const double *fric, double *v_out, double *g_out,

@@ -19,9 +19,10 @@ owt_handle::~owt_handle() {
     if (e) cudaEventDestroy(e);
   if (hs.ready) {
     for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamSynchronize(q);
-    for (cudaEvent_t e : hs.landed)
-      if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {hs.v_done, hs.q_done, hs.up_done, hs.tx_done, hs.after_modes, hs.down_done})
+    for (int j = 0; j < HostStep::kChunks; ++j)
+      for (cudaEvent_t e : {hs.landed[j], hs.v_done[j], hs.q_done[j], hs.tx_done[j]})
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {hs.up_done, hs.after_modes, hs.down_done})
       if (e) cudaEventDestroy(e);
     for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamDestroy(q);
   }

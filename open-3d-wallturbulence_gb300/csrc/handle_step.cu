@@ -57,12 +57,23 @@ NLArgs owt_handle::nl_args(bool record_mean) const {
 // The mean mode runs on a second stream beside the mode kernel (they touch
 // disjoint data); both read the counter before it advances.
 void owt_handle::enqueue_step(cudaEvent_t after_modes) {
+  step_begin();
+  stage_modes();
+  if (after_modes) ck(cudaEventRecord(after_modes, st), "after modes");
+  step_finish();
+}
+
+// The mean mode on the second stream, beside the mode kernel.
+void owt_handle::step_begin() {
   ck(cudaEventRecord(ev_fork, st), "fork");
   ck(cudaStreamWaitEvent(st2, ev_fork, 0), "fork wait");
   stage_mean(true, st2);
   ck(cudaEventRecord(ev_join, st2), "join");
-  stage_modes();
-  if (after_modes) ck(cudaEventRecord(after_modes, st), "after modes");
+}
+
+// After the mode kernel: join the mean mode, advance the counter, the Lamb
+// vector and the nonlinear source.
+void owt_handle::step_finish() {
   ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launch_advance(d_step, st);
   const XformArgs xa = xform_args();
@@ -97,6 +108,7 @@ void owt_handle::stage_modes() {
 ModeArgs owt_handle::mode_args() const {
   ModeArgs a{};
   a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.U = Uq;
+  a.u0 = 0; a.u1 = Uq;
   a.inv_dt = 1.0 / p.dt; a.nu = p.nu;
   a.kx = kx; a.kz = kz; a.c11 = c11; a.c21 = c21; a.c22 = c22;
   a.v_ring = v_ring; a.g_ring = g_ring; a.hv_ring = hv_ring; a.hg_ring = hg_ring; a.q_ring = q_ring;
@@ -224,6 +236,7 @@ void owt_handle::autotune_modes() {
 void owt_handle::recompute_dirty_q(cudaStream_t on) {
   DY2Args a{};
   a.NY = NY; a.M = M;
+  a.m0 = 0; a.mcount = M;
   a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
   a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
   a.c21 = c21; a.c22 = c22;
@@ -449,51 +462,42 @@ void owt_handle::host_step_prepare() {
   ck(cudaStreamCreateWithFlags(&hs.aux, cudaStreamNonBlocking), "stream");
   ck(cudaStreamCreateWithPriority(&hs.tx, cudaStreamNonBlocking, hi), "stream");
   ck(cudaStreamCreateWithPriority(&hs.down, cudaStreamNonBlocking, hi), "stream");
-  for (int i = 0; i < 12; ++i) {
-    hs.stage[i] = dalloc<double2>(fs, owned);
-    ck(cudaEventCreateWithFlags(&hs.landed[i], cudaEventDisableTiming), "event");
-  }
+  for (int i = 0; i < 12; ++i) hs.stage[i] = dalloc<double2>(fs, owned);
   for (int b = 0; b < 2; ++b) hs.dstage[b] = dalloc<double2>(fs, owned);
-  for (cudaEvent_t *e : {&hs.v_done, &hs.q_done, &hs.up_done, &hs.tx_done, &hs.after_modes, &hs.down_done})
+  for (int j = 0; j < HostStep::kChunks; ++j)
+    for (cudaEvent_t *e : {&hs.landed[j], &hs.v_done[j], &hs.q_done[j], &hs.tx_done[j]})
+      ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
+  for (cudaEvent_t *e : {&hs.up_done, &hs.after_modes, &hs.down_done})
     ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
   hs.ready = true;
 }
 
-// Uploads: every field has a staging buffer of its own, so the twelve
-// host-to-device copies run back to back on the copy stream; each field's
-// layout transpose into its ring slot follows its copy on a high-priority
-// stream (whose blocks the scheduler places ahead of those of long kernels).
-// The DY2 v history of the three uploaded v levels is re-derived on a third
-// stream while the other nine fields are still arriving.  Downloads: the new
-// v and omega_y are final after the mode kernel, so their transposes (high
-// priority) and copies run beside the transforms of the same step.
+// Uploads, by chunks of Fourier modes: the modes with |kz| in a range are
+// the host rows kz of that range and of its negative partners, contiguous in
+// the reference layout.  Chunk by chunk, the twelve fields' rows are copied
+// back to back into staging buffers of their own (one per field), then
+// transposed into their ring slots on a high-priority stream (whose blocks
+// the scheduler places ahead of those of long kernels), the DY2 v history of
+// the chunk's modes is re-derived on a third stream, and the mode kernel
+// runs on the chunk's unique modes while the next chunks arrive.  One chunk
+// (everything) when the mode-kernel variant in use is not the quad mapping,
+// whose unique-mode ranges the chunks are.  Downloads: the new v and omega_y
+// are final after the mode kernel, so their transposes (high priority) and
+// copies run beside the transforms of the same step.
 void owt_handle::step_host(const double *const *hist, const double *means, const double *fric, double *v_out,
                            double *g_out, double *fric_out) {
   host_step_prepare();
   ensure_tuned();
   ck(cudaStreamSynchronize(st), "host step");
-  double2 *rings[4] = {v_ring, g_ring, hv_ring, hg_ring};
-  for (int i = 0; i < 12; ++i) {
-    ck(cudaMemcpyAsync(hs.stage[i], hist[i], fs * sizeof(double2), cudaMemcpyHostToDevice, hs.up), "H2D");
-    ck(cudaEventRecord(hs.landed[i], hs.up), "landed");
-  }
+  const int variant = forced_variant >= 0 ? forced_variant : modes_variant;
+  const bool quad = modes_sparse() && !sparse_v6 && variant >= modes_pair_count();
+  const int want = host_chunks > 0 ? host_chunks : HostStep::kDefaultChunks;
+  const int nchunk = quad ? std::min(std::min(want, HostStep::kChunks), NZH + 1) : 1;
+  // means first (the mean-mode kernel starts with the step)
   for (int w = 0; w < OWT_NUM_MEANS; ++w)
     ck(cudaMemcpyAsync(mean_ptr(w), means + 2 * (size_t)w * NY, NY * sizeof(double2), cudaMemcpyHostToDevice, hs.up),
        "H2D");
-  ck(cudaEventRecord(hs.up_done, hs.up), "uploads done");
-  for (int i = 0; i < 12; ++i) {
-    ck(cudaStreamWaitEvent(hs.tx, hs.landed[i], 0), "landed wait");
-    launch_transpose(hs.stage[i], ring_level(rings[i / 3], i % 3), M, NY, hs.tx);  // [M][NY] -> [NY][M]
-    ++launches;
-    if (i == 2) {  // the three v levels are in place: DY2 v on the side
-      ck(cudaEventRecord(hs.v_done, hs.tx), "v done");
-      ck(cudaStreamWaitEvent(hs.aux, hs.v_done, 0), "v wait");
-      q_dirty[0] = q_dirty[1] = q_dirty[2] = true;
-      recompute_dirty_q(hs.aux);
-      ck(cudaEventRecord(hs.q_done, hs.aux), "q done");
-    }
-  }
-  ck(cudaEventRecord(hs.tx_done, hs.tx), "transposes done");
+  ck(cudaEventRecord(hs.up_done, hs.up), "means done");
   {
     double fx[3], fz[3];
     for (int l = 0; l < 3; ++l) {
@@ -503,12 +507,87 @@ void owt_handle::step_host(const double *const *hist, const double *means, const
     ck(cudaMemcpyAsync(fx_ring, fx, sizeof(fx), cudaMemcpyHostToDevice, st), "H2D");
     ck(cudaMemcpyAsync(fz_ring, fz, sizeof(fz), cudaMemcpyHostToDevice, st), "H2D");
   }
-  for (cudaEvent_t e : {hs.up_done, hs.tx_done, hs.q_done}) ck(cudaStreamWaitEvent(st, e, 0), "uploads wait");
+  double2 *rings[4] = {v_ring, g_ring, hv_ring, hg_ring};
+  const size_t row = (size_t)NXH * NY;  // complex values of one kz row, reference layout
+  // row blocks [k0, k1) of chunk j: |kz| in [a, b) for kz <= NZH, and the
+  // negative partners NZ - |kz| for 1 <= |kz| < NZH
+  auto blocks = [&](int j, int (&k0)[2], int (&k1)[2]) {
+    if (nchunk == 1) {
+      k0[0] = 0; k1[0] = NZ; k0[1] = k1[1] = 0;
+      return;
+    }
+    const int a = (NZH + 1) * j / nchunk, b = (NZH + 1) * (j + 1) / nchunk;
+    k0[0] = a; k1[0] = b;
+    const int pa = std::max(a, 1), pb = std::min(b, NZH);
+    k0[1] = pb > pa ? NZ - pb + 1 : 0;
+    k1[1] = pb > pa ? NZ - pa + 1 : 0;
+  };
+  for (int j = 0; j < nchunk; ++j) {
+    int k0[2], k1[2];
+    blocks(j, k0, k1);
+    for (int i = 0; i < 12; ++i)
+      for (int q = 0; q < 2; ++q)
+        if (k1[q] > k0[q])
+          ck(cudaMemcpyAsync(hs.stage[i] + k0[q] * row, hist[i] + 2 * k0[q] * row, (k1[q] - k0[q]) * row * sizeof(double2),
+                             cudaMemcpyHostToDevice, hs.up), "H2D");
+    ck(cudaEventRecord(hs.landed[j], hs.up), "landed");
+  }
+  ck(cudaStreamWaitEvent(st, hs.up_done, 0), "means wait");
   ++state_version;
   initialized = true;
-  // the new v, omega_y land in the slot that becomes level 0 after the step
-  const int hn = (head() + 2) % 3;
-  enqueue_step(hs.after_modes);
+  const int hn = (head() + 2) % 3;  // the new v, omega_y land in the slot that becomes level 0
+  step_begin();
+  for (int j = 0; j < nchunk; ++j) {
+    int k0[2], k1[2];
+    blocks(j, k0, k1);
+    ck(cudaStreamWaitEvent(hs.tx, hs.landed[j], 0), "landed wait");
+    for (int i = 0; i < 12; ++i) {
+      for (int q = 0; q < 2; ++q)
+        if (k1[q] > k0[q]) {
+          const int m0 = k0[q] * NXH, nm = (k1[q] - k0[q]) * NXH;
+          launch_transpose_ld(hs.stage[i] + (size_t)m0 * NY, ring_level(rings[i / 3], i % 3) + m0, nm, NY, M, hs.tx);
+          ++launches;
+        }
+      if (i == 2) {  // the chunk's v levels are in place: their DY2 v on the side
+        ck(cudaEventRecord(hs.v_done[j], hs.tx), "v done");
+        ck(cudaStreamWaitEvent(hs.aux, hs.v_done[j], 0), "v wait");
+        for (int q = 0; q < 2; ++q)
+          if (k1[q] > k0[q]) {
+            DY2Args a{};
+            a.NY = NY; a.M = M;
+            a.m0 = k0[q] * NXH; a.mcount = (k1[q] - k0[q]) * NXH;
+            a.ab1 = b1.ab; a.piv1 = b1.piv; a.ab2 = b2.ab; a.piv2 = b2.piv;
+            a.b1_col = b1_col; a.b1_val = b1_val; a.b2_col = b2_col; a.b2_val = b2_val;
+            a.c21 = c21; a.c22 = c22;
+            double2 *scr[3] = {tmpA, tmpB, tmpC};
+            for (int l = 0; l < 3; ++l) {
+              a.in[l] = ring_level(v_ring, l);
+              a.out[l] = ring_level(q_ring, l);
+              a.scr[l] = scr[l];
+            }
+            a.nf = 3;
+            launch_dy2(a, hs.aux);
+            ++launches;
+          }
+        ck(cudaEventRecord(hs.q_done[j], hs.aux), "q done");
+      }
+    }
+    ck(cudaEventRecord(hs.tx_done[j], hs.tx), "transposes done");
+    ck(cudaStreamWaitEvent(st, hs.tx_done[j], 0), "transposes wait");
+    ck(cudaStreamWaitEvent(st, hs.q_done[j], 0), "DY2 v wait");
+    if (nchunk == 1) {
+      stage_modes();
+    } else {
+      ModeArgs a = mode_args();
+      a.u0 = ((NZH + 1) * j / nchunk) * NXH;
+      a.u1 = ((NZH + 1) * (j + 1) / nchunk) * NXH;
+      launch_modes(a, bv.kl, bv.ku, bg.kl, bg.ku, true, variant, st);
+    }
+    ++launches;
+  }
+  q_dirty[0] = q_dirty[1] = q_dirty[2] = false;
+  ck(cudaEventRecord(hs.after_modes, st), "after modes");
+  step_finish();
   ++steps;
   ck(cudaStreamWaitEvent(hs.down, hs.after_modes, 0), "modes wait");
   double *outs[2] = {v_out, g_out};

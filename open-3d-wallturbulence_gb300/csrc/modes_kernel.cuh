@@ -30,9 +30,9 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
   // share one factorization, so four adjacent lanes read the same factors.
   int m, comp, k, i, kabs;
   if (QUAD) {
-    const int uq = tid >> 2, r = tid & 3, sgn = r >> 1;
+    const int uq = a.u0 + (tid >> 2), r = tid & 3, sgn = r >> 1;
     comp = r & 1;
-    if (uq >= a.U) return;
+    if (uq >= a.u1) return;
     kabs = uq / a.NXH;
     i = uq - kabs * a.NXH;
     if (sgn == 1 && (kabs == 0 || kabs == a.NZH)) return;  // these have no -kz partner

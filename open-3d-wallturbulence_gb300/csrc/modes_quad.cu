@@ -29,7 +29,7 @@ int modes_quad_count() { return (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 const char *modes_quad_name(int v) { return kVariants[v].name; }
 void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st) {
   const Variant &x = kVariants[v];
-  const long long threads = 4 * (long long)a.U;
+  const long long threads = 4 * (long long)(a.u1 - a.u0);
   x.kernel<<<(unsigned)((threads + x.block - 1) / x.block), x.block, 0, st>>>(a);
 }
 

@@ -646,8 +646,8 @@ void launch_dapply(const DApplyArgs &a, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_dy2(DY2Args a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = tid >> 1, comp = tid & 1, f = blockIdx.y;
-  if (m >= a.M) return;
+  if ((tid >> 1) >= a.mcount) return;
+  const int m = a.m0 + (tid >> 1), comp = tid & 1, f = blockIdx.y;
   const int M = a.M, NY = a.NY;
   auto E = [&](int j) { return 2 * ((size_t)j * M + m) + comp; };
   const double *in = reinterpret_cast<const double *>(a.in[f]);
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(128) k_dy2(DY2Args a) {
 }
 
 void launch_dy2(const DY2Args &a, cudaStream_t st) {
-  k_dy2<<<dim3((unsigned)((2 * (long long)a.M + 127) / 128), a.nf), 128, 0, st>>>(a);
+  k_dy2<<<dim3((unsigned)((2 * (long long)a.mcount + 127) / 128), a.nf), 128, 0, st>>>(a);
 }
 
 // Elementwise helpers --------------------------------------------------------
@@ -823,6 +823,26 @@ __global__ void k_transpose(const double2 *__restrict__ in, double2 *__restrict_
 void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st) {
   dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
   k_transpose<<<g, b, 0, st>>>(in, out, rows, cols);
+}
+// A block of rows of the reference layout into the device layout: rows r of
+// in ([rows][cols]) become columns r of out, whose rows are ldo values apart.
+__global__ void k_transpose_ld(const double2 *__restrict__ in, double2 *__restrict__ out, int rows, int cols,
+                               int ldo) {
+  __shared__ double2 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = by + r, col = bx + threadIdx.x;
+    if (row < rows && col < cols) tile[r][threadIdx.x] = in[(size_t)row * cols + col];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int orow = bx + r, ocol = by + threadIdx.x;
+    if (orow < cols && ocol < rows) out[(size_t)orow * ldo + ocol] = tile[threadIdx.x][r];
+  }
+}
+void launch_transpose_ld(const double2 *in, double2 *out, int rows, int cols, int ldo, cudaStream_t st) {
+  dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose_ld<<<g, b, 0, st>>>(in, out, rows, cols, ldo);
 }
 // Physical fields: [y][z][x] (device) <-> [z][x][y] (the reference's
 // Field<double> layout), a rows x cols transpose of doubles.

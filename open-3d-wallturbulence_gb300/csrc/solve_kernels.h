@@ -31,6 +31,7 @@ inline cudaError_t raise_smem_limit(F *func, size_t bytes) {
 
 struct ModeArgs {
   int NY, NZ, NXH, NZH, M, U;
+  int u0, u1;  // quad mapping: unique modes u0 <= u < u1 only (0, U: all)
   double inv_dt, nu;
   const double *kx, *kz, *c11, *c21, *c22;
   double2 *v_ring, *g_ring, *hv_ring, *hg_ring, *q_ring;  // 3 slots each, [slot][y][mode]
@@ -90,6 +91,7 @@ struct DApplyArgs {
 
 struct DY2Args {
   int NY, M, nf;  // nf fields (at most 3)
+  int m0, mcount; // modes m0 .. m0 + mcount - 1 (0, M: all)
   const double2 *in[3];
   double2 *out[3], *scr[3];  // scr: one field of scratch each
   const double *ab1, *ab2; const uint8_t *piv1, *piv2;
@@ -141,6 +143,7 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
                         const double *t2, const double *s1, const double *s2, double *rscale, int *info,
                         cudaStream_t st, int kernel = 0);
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
+int modes_pair_count();  // variants below this index use the pair mapping, the others the quad mapping
 void launch_modes_sixth(const ModeArgs &a, cudaStream_t st);  // masked solve with the sixth-order fill
 int modes_variant_count();
 const char *modes_variant_name(int v);
@@ -160,6 +163,8 @@ void launch_friction(const double2 *d1u, const double2 *d1w, const double *c11, 
 void launch_lamb_mean_shift(double2 *lx_ring, double2 *lz_ring, const double2 *lx, const double2 *lz, int NY, int M,
                             const long long *step, cudaStream_t st);
 void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaStream_t st);
+// the same with the output rows ldo values apart: out[c * ldo + r] = in[r * cols + c]
+void launch_transpose_ld(const double2 *in, double2 *out, int rows, int cols, int ldo, cudaStream_t st);
 // the same for a rows x cols matrix of doubles
 void launch_transpose_real(const double *in, double *out, int rows, int cols, cudaStream_t st);
 void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,

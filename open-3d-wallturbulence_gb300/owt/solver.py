@@ -234,6 +234,11 @@ class GpuSolver:
         (OWT_OPT_MEAN_SPLIT)."""
         self._chk(self.L.owt_set_option(self.h, 4, 1 if on else 0))
 
+    def set_host_chunks(self, n):
+        """Chunks of Fourier modes owt_time_integration_host pipelines its uploads
+        over (0: the library's default; OWT_OPT_HOST_CHUNKS)."""
+        self._chk(self.L.owt_set_option(self.h, 5, int(n)))
+
     def force_modes_variant(self, v):
         """Run mode-kernel variant v (-1: the autotuned one)."""
         self._chk(self.L.owt_set_option(self.h, 2, int(v)))

@@ -185,20 +185,23 @@ def test_state_keep_and_restore_on_device(gpu_lib, run):
     assert s.step == first[3]
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_host_state_step_equals_device_step(gpu_lib, precision):
+@pytest.mark.parametrize("precision,variant", [("fp64", None), ("mixed", None), ("fp64", "quad"), ("mixed", "quad")])
+def test_host_state_step_equals_device_step(gpu_lib, precision, variant):
     """owt_time_integration_host (one step on a host-held state, copies
     overlapped with the device work) gives the bits of uploading the same
     state with the set-field calls and stepping, whatever the receiving
     handle's own ring position: the returned v, omega_y and friction, and the
-    handle's state afterwards, on two calls in a row.  Both re-derive the
+    handle's state afterwards, on two calls in a row.  With a quad-mapping
+    mode kernel the call pipelines the uploads with the mode kernel over
+    chunks of Fourier modes; the result is the same bits.  Both re-derive the
     DY2 v history of the uploaded v levels, which an uninterrupted run
     carries from its own solves, so against the uninterrupted step they
     agree to the one-step bound (1e-10)."""
     from owt.ic import seeded_velocity
     from owt.params import CaseParams
     from owt.solver import GpuSolver
-    p = CaseParams(dt=0.002, dkx=1.0, dkz=2.0, NX=32, NY=33, NZ=24, alpha_mesh=2.2, nu=1e-4)
+    # NY = 129: long enough for the masked (sparse) solves the quad mapping serves
+    p = CaseParams(dt=0.002, dkx=1.0, dkz=2.0, NX=32, NY=129 if variant else 33, NZ=24, alpha_mesh=2.2, nu=1e-4)
     means_names = ("lmbx_mean_0", "lmbx_mean_1", "lmbx_mean_2", "lmbz_mean_0", "lmbz_mean_1", "lmbz_mean_2",
                    "velx_mean_0", "velx_mean_1", "velx_mean_2", "velz_mean_0", "velz_mean_1", "velz_mean_2")
     a = GpuSolver(p, precision=precision)
@@ -217,6 +220,9 @@ def test_host_state_step_equals_device_step(gpu_lib, precision):
     c.time_Integration(1)
     a.time_Integration(1)
     b = GpuSolver(p, precision=precision)
+    if variant == "quad":
+        assert b.info("sparse_solve") == 1
+        b.force_modes_variant(b.info("modes_variants") - 1)  # the last variant maps threads by quads
     b.init_fields(*seeded_velocity(p, seed=9))
     b.time_Integration(1)  # a different ring position than c's
     for rep in range(2):
