@@ -197,9 +197,15 @@ __device__ __forceinline__ void xlamb_stage(const XformArgs &a, size_t line0, fl
   }
 }
 
-template <int A, int B, int P>
-__device__ __forceinline__ void xlamb_r_group(const XformArgs &a, const size_t line0, const float2 *Rin,
-                                              float2 *R0, float2 *R1, const float2 *tw) {
+// One group of P (y, z) lines in R (3P lines of shared memory).  Lines, in
+// turn: the 3P backward transposes; the 3P physical lines (field pairs); in
+// place, the 3P/2 product pairs in lines 0 .. 3P/2 - 1; their forward
+// transposes in lines 3P/2 .. 3P - 1; their spectra in lines 0 .. 3P/2 - 1.
+// after_input() runs once every thread has read Rin (the next group's input
+// may then start arriving there).
+template <int A, int B, int P, class AfterInput>
+__device__ __forceinline__ void xlamb_r_group(const XformArgs &a, const size_t line0, const float2 *Rin, float2 *R,
+                                              const float2 *tw, AfterInput after_input) {
   using G = Line2<A, B>;
   static_assert(P % 2 == 0, "lz lines pack two (y, z) lines each");
   constexpr int NF = P + P / 2, L = G::L;
@@ -217,55 +223,69 @@ __device__ __forceinline__ void xlamb_r_group(const XformArgs &a, const size_t l
     dft<A, true, float>(x);
     twiddle_row<A, true>(x, t, tw);
 #pragma unroll
-    for (int r = 0; r < A; ++r) R0[q * G::LS + r * G::RS + t] = x[r];
+    for (int r = 0; r < A; ++r) R[q * G::LS + r * G::RS + t] = x[r];
   }
   __syncthreads();
+  after_input();
   // 2. backward pass 2: point t + A r of each packed line (a + i b = the two fields)
   float2 y[B];
   if (t < A) {
 #pragma unroll
-    for (int r = 0; r < B; ++r) y[r] = R0[q * G::LS + t * G::RS + r];
+    for (int r = 0; r < B; ++r) y[r] = R[q * G::LS + t * G::RS + r];
     dft<B, true, float>(y);
   }
   __syncthreads();
   if (t < A) {
 #pragma unroll
-    for (int r = 0; r < B; ++r) R0[q * G::LS + t + A * r] = y[r];
+    for (int r = 0; r < B; ++r) R[q * G::LS + t + A * r] = y[r];
   }
   __syncthreads();
   // 3. lamb = u x omega (no fused multiply-add, as the reference's separate
-  // products), packed as (lx + i ly) per line and (lz_l + i lz_l+1)
-  for (int idx = threadIdx.x; idx < P * L; idx += blockDim.x) {
-    const int l = idx / L, xx = idx - l * L;
-    const float2 uv = R0[(0 * P + l) * G::LS + xx], wox = R0[(1 * P + l) * G::LS + xx],
-                 oyz = R0[(2 * P + l) * G::LS + xx];
-    const float u = uv.x, v = uv.y, w = wox.x, ox = wox.y, oy = oyz.x, oz = oyz.y;
-    const float lx = __fmul_rn(v, oz) - __fmul_rn(w, oy);
-    const float ly = __fmul_rn(w, ox) - __fmul_rn(u, oz);
-    const float lz = __fmul_rn(u, oy) - __fmul_rn(v, ox);
-    R1[l * G::LS + xx] = make_float2(lx, ly);
-    float *pz = reinterpret_cast<float *>(&R1[(P + l / 2) * G::LS + xx]);
-    pz[l & 1] = lz;
+  // products), packed as (lx + i ly) in line l and (lz_l + i lz_l+1) in line
+  // P + l/2, in place: one thread owns point xx of every line, reading all
+  // its values before writing any
+  for (int xx = threadIdx.x; xx < L; xx += blockDim.x) {
+    float2 uv[P], wox[P], oyz[P];
+#pragma unroll
+    for (int l = 0; l < P; ++l) {
+      uv[l] = R[(0 * P + l) * G::LS + xx];
+      wox[l] = R[(1 * P + l) * G::LS + xx];
+      oyz[l] = R[(2 * P + l) * G::LS + xx];
+    }
+#pragma unroll
+    for (int l = 0; l < P; l += 2) {
+      float lz[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float u = uv[l + h].x, v = uv[l + h].y, w = wox[l + h].x, ox = wox[l + h].y, oy = oyz[l + h].x,
+                    oz = oyz[l + h].y;
+        const float lx = __fmul_rn(v, oz) - __fmul_rn(w, oy);
+        const float ly = __fmul_rn(w, ox) - __fmul_rn(u, oz);
+        lz[h] = __fmul_rn(u, oy) - __fmul_rn(v, ox);
+        R[(l + h) * G::LS + xx] = make_float2(lx, ly);
+      }
+      R[(P + l / 2) * G::LS + xx] = make_float2(lz[0], lz[1]);
+    }
   }
   __syncthreads();
-  // 4. forward pass 1 of the NF product pairs
+  // 4. forward pass 1 of the NF product pairs, transposes into lines NF + q
   if (q < NF && t < B) {
     float2 x[A];
 #pragma unroll
-    for (int r = 0; r < A; ++r) x[r] = R1[q * G::LS + t + B * r];
+    for (int r = 0; r < A; ++r) x[r] = R[q * G::LS + t + B * r];
     dft<A, false, float>(x);
     twiddle_row<A, false>(x, t, tw);
 #pragma unroll
-    for (int r = 0; r < A; ++r) R0[q * G::LS + r * G::RS + t] = x[r];
+    for (int r = 0; r < A; ++r) R[(NF + q) * G::LS + r * G::RS + t] = x[r];
   }
   __syncthreads();
-  // 5. forward pass 2: spectrum slot t + A r
+  // 5. forward pass 2: spectrum slot t + A r, into line q
   if (q < NF && t < A) {
 #pragma unroll
-    for (int r = 0; r < B; ++r) y[r] = R0[q * G::LS + t * G::RS + r];
+    for (int r = 0; r < B; ++r) y[r] = R[(NF + q) * G::LS + t * G::RS + r];
     dft<B, false, float>(y);
 #pragma unroll
-    for (int r = 0; r < B; ++r) R1[q * G::LS + t + A * r] = y[r];
+    for (int r = 0; r < B; ++r) R[q * G::LS + t + A * r] = y[r];
   }
   __syncthreads();
   // 6. unpack the real-pair spectra, keep kx < NXH, scale by 1/NX2
@@ -277,13 +297,13 @@ __device__ __forceinline__ void xlamb_r_group(const XformArgs &a, const size_t l
     if (line >= nlines) continue;
     const int mc = (km == 0) ? 0 : d.NX2 - km;
     {
-      const float2 zm = R1[l * G::LS + km], zc = R1[l * G::LS + mc];
+      const float2 zm = R[l * G::LS + km], zc = R[l * G::LS + mc];
       // Xa = (Z[m] + conj Z[-m]) / 2 ; Xb = (Z[m] - conj Z[-m]) / (2i)
       lb[line * d.NXH + km] = make_float2((zm.x + zc.x) * half, (zm.y - zc.y) * half);
       lb[fstride + line * d.NXH + km] = make_float2((zm.y + zc.y) * half, (zc.x - zm.x) * half);
     }
     {
-      const float2 zm = R1[(P + l / 2) * G::LS + km], zc = R1[(P + l / 2) * G::LS + mc];
+      const float2 zm = R[(P + l / 2) * G::LS + km], zc = R[(P + l / 2) * G::LS + mc];
       const float2 val = (l & 1) ? make_float2((zm.y + zc.y) * half, (zc.x - zm.x) * half)
                                  : make_float2((zm.x + zc.x) * half, (zm.y - zc.y) * half);
       lb[2 * fstride + line * d.NXH + km] = val;
@@ -303,18 +323,20 @@ template <int A, int B>
 __global__ void __launch_bounds__(kRegTX * Line2<A, B>::T) k_zfwd_r(const __grid_constant__ XformArgs a) {
   zfwd_r_body<A, B>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-// Shared memory of the persistent x pass: R0 (3P lines: transposes, then
-// the physical lines), R1 (3P/2 lines: the product pairs, then their
-// spectra), two input buffers of 6 P NXH values, the twiddle table.
+// Shared memory of the persistent x pass: R (3P lines: transposes, physical
+// lines, product pairs, their transposes and spectra), the input of one
+// group (6 P NXH values), the twiddle table.
 template <int A, int B, int P>
 struct XSmem {
   using G = Line2<A, B>;
-  static constexpr int R0 = 0, R1 = 3 * P * G::LS, IN = R1 + (P + P / 2) * G::LS, INSZ = 6 * P * (G::L / 3),
-                       TW = IN + 2 * INSZ, TOTAL = TW + G::L;
+  static constexpr int R = 0, IN = 3 * P * G::LS, INSZ = 6 * P * (G::L / 3), TW = IN + INSZ, TOTAL = TW + G::L;
 };
 
-// The groups g0, g0 + step, ... < ngroups of one channel (a); `args(g)` gives
-// the arguments and first line of group g (several channels in the batch).
+// The groups g0, g0 + step, ... < ngroups; `args(g)` gives the arguments and
+// first line of group g (several channels in the batch).  The input of the
+// next group is copied (cp.async) into the one input buffer as soon as
+// every thread has read the current one, so it arrives while the current
+// group is transformed.
 template <int A, int B, int P, class Args>
 __device__ __forceinline__ void xlamb_r_run(int g0, int step, int ngroups, const float2 *twsrc, Args args) {
   using S = XSmem<A, B, P>;
@@ -323,26 +345,26 @@ __device__ __forceinline__ void xlamb_r_run(int g0, int step, int ngroups, const
   float2 *sm = reinterpret_cast<float2 *>(smraw);
   float2 *tw = sm + S::TW;
   for (int k = threadIdx.x; k < Line2<A, B>::L; k += blockDim.x) tw[k] = twsrc[k];
-  int it = 0;
   if (g0 < ngroups) {
     size_t line0;
     const XformArgs &a0 = args(g0, line0);
     xlamb_stage<P>(a0, line0, sm + S::IN);
   }
   cp_async_commit();
-  for (int g = g0; g < ngroups; g += step, ++it) {
-    const int gn = g + step;
-    if (gn < ngroups) {
-      size_t line0;
-      const XformArgs &an = args(gn, line0);
-      xlamb_stage<P>(an, line0, sm + S::IN + ((it + 1) & 1) * S::INSZ);
-    }
-    cp_async_commit();
-    cp_async_wait<1>();
+  for (int g = g0; g < ngroups; g += step) {
+    cp_async_wait<0>();
     __syncthreads();
     size_t line0;
     const XformArgs &ag = args(g, line0);
-    xlamb_r_group<A, B, P>(ag, line0, sm + S::IN + (it & 1) * S::INSZ, sm + S::R0, sm + S::R1, tw);
+    const int gn = g + step;
+    xlamb_r_group<A, B, P>(ag, line0, sm + S::IN, sm + S::R, tw, [&] {
+      if (gn < ngroups) {
+        size_t nline0;
+        const XformArgs &an = args(gn, nline0);
+        xlamb_stage<P>(an, nline0, sm + S::IN);
+      }
+      cp_async_commit();
+    });
   }
   cp_async_wait<0>();
 }
