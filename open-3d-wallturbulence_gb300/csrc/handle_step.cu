@@ -26,7 +26,6 @@ XformArgs owt_handle::xform_args() const {
   a.fs = fs;
   a.step = d_step;
   a.mean_split = (precision == OWT_PREC_MIXED && mean_split) ? 1 : 0;
-  for (int f = 0; f < 3; ++f) a.lm[f] = lm + (size_t)f * fs;
   a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
   a.zbuf = zbuf; a.lbuf = lbuf;
   a.px = px; a.pz = pz;
@@ -76,22 +75,7 @@ void owt_handle::step_begin() {
 void owt_handle::step_finish() {
   ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launch_advance(d_step, st);
-  const XformArgs xa = xform_args();
-  int nx = 3;
-  if (xa.mean_split) {
-    // the FP64 mean-flow terms beside the FP32 z backward and x pass
-    ck(cudaEventRecord(ev_fork2, st), "fork");
-    ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
-    launch_lamb_part(xa, precision, 3, st2);
-    ck(cudaEventRecord(ev_join2, st2), "join");
-    launch_lamb_part(xa, precision, 0, st);
-    launch_lamb_part(xa, precision, 1, st);
-    ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
-    launch_lamb_part(xa, precision, 2, st);
-    nx = 4;
-  } else {
-    nx = launch_lamb(xa, precision, st);
-  }
+  const int nx = launch_lamb(xform_args(), precision, st);
   launch_nl(nl_args(true), st);
   launches += 4 + nx;
 }
@@ -321,7 +305,7 @@ void owt_handle::init_seeded(uint64_t seed, double rms) {
   a.seed = seed;
   a.kmin = std::min(p.dkx, p.dkz);
   a.kx = kx; a.kz = kz; a.y = ygrid; a.c11 = c11; a.wy = wy;
-  a.coef = lm;  // 3 NY M >= 12 M values
+  a.coef = reinterpret_cast<double2 *>(zbuf);  // >= 3 NY M values, free until the transforms
   double2 *v0 = ring_level(v_ring, 0);
   launches += launch_ic_fields(a, v0, tmpC, st);
   dapply(1, v0, tmpA);

@@ -16,13 +16,14 @@
 //  k_zfwd  : per (y, kx tile, field) -- forward FFT of length NZ2, keep slots
 //            k < NZH and NZ + k (k < NZH) -> kz index k + NZH, / NZ2
 //            (FFT.cpp:177-188).  The Nyquist row is kept on this path.
-//  k_mean_lamb (mixed precision only): the FP64 mean-flow terms that the
-//            FP32 transforms leave out, added element-wise.
+//            FP32 (mixed precision): plus the mean-flow terms the FP32
+//            transforms leave out, element by element (mean_flow.cuh).
 //
 // Between kernels the z-padded, x-truncated planes live in HBM as
 // [field][y][z][kx] complex<T>.  T = double (FP64 step) or float (mixed).
 #include <cuda_runtime.h>
 
+#include "mean_flow.cuh"
 #include "owt_device.cuh"
 #include "solve_kernels.h"
 
@@ -158,98 +159,37 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
   __syncthreads();
   const cpx<T> *r = fft_lines<T, false, R5>(bufa, bufb, TX, ls, a.pz, reinterpret_cast<const cpx<T> *>(a.twz));
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
-  // mixed precision (FP32 transforms): plus the FP64 mean-flow terms
-  // k_mean_lamb wrote; the FP64 instances carry no such epilogue
-  constexpr bool kSplit = sizeof(T) == sizeof(float);
-  const double2 *lm = (kSplit && a.mean_split) ? a.lm[f] + (size_t)j * d.NZ * d.NXH : nullptr;
-  const double sc = a.inv_nz2;
-  for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
-    const int kz = idx / TX, c = idx - kz * TX;
-    if (i0 + c < d.NXH) {
-      const int slot = kz < d.NZH ? kz : kz + d.NZH;
-      const double2 v = to_d(r[c * ls + sw<T>(slot)]);
-      const size_t at = (size_t)kz * d.NXH + i0 + c;
-      // explicit roundings: the batched and the one-channel kernels must
-      // give the same bits whatever each compilation contracts
-      double2 o = make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
-      if (kSplit && lm) {
-        const double2 l = lm[at];
-        o.x = __dadd_rn(o.x, l.x);
-        o.y = __dadd_rn(o.y, l.y);
-      }
-      dst[at] = o;
-    }
-  }
-}
-
-// Mixed precision: the interaction of the mean flow with the fluctuations
-// that the FP32 transforms leave out (mode (0, 0) is zeroed in k_zback), in
-// FP64, written to lm for the z forward to add: Ubar x om + u x Obar at every
-// mode and y, Ubar x Obar at (0, 0), zero on the Nyquist row (it never reaches
-// physical space).  It reads only the step's fields, so it runs beside the z
-// backward and the x pass.
-// Ubar, Obar are the real parts of the (0, 0) modes of row j; the kx = 0
-// column enters through its Hermitian part, as the real-part extraction of
-// the x transform makes it enter the physical product.  Grid: (modes / 256,
-// NY); one thread per mode of row j (the grid's y), all three components.
-__device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx, const int j) {
-  const XformDims d = a.d;
-  const int M = d.NZ * d.NXH;
-  const int m = bx * 256 + threadIdx.x;
-  if (m >= M) return;
-  const int kz = m / d.NXH, kx = m - kz * d.NXH;
-  const size_t row = (size_t)j * M, e = row + m;
-  if (kz == d.NZH) {
-    for (int f = 0; f < 3; ++f) a.lm[f][e] = make_double2(0.0, 0.0);
-    return;
-  }
-  const int hd = ring_head(*a.step);
-  const double2 *base[6];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) {
-    base[q] = a.in[q] + row;
-    if (a.ring_mask & (1 << q)) base[q] += (size_t)hd * a.fs;
-  }
-  {
-    double Ub[3], Ob[3];
-    double2 F[6];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) { Ub[q] = base[q][0].x; Ob[q] = base[3 + q][0].x; }
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      const double2 x = base[q][m];
-      if (kx != 0) {
-        F[q] = x;
-      } else {
-        const double2 y = base[q][(kz == 0 ? 0 : d.NZ - kz) * d.NXH];
-        F[q] = make_double2(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // FP32 transforms: the 1/NZ2 normalisation and (mean split) the
+    // mean-flow terms of mean_flow.cuh in FP32, then the exact widening
+    const float sc = (float)a.inv_nz2;
+    MeanRow mr;
+    if (a.mean_split) mr = mean_row(a, j, f);
+    for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
+      const int kz = idx / TX, c = idx - kz * TX;
+      if (i0 + c < d.NXH) {
+        const int slot = kz < d.NZH ? kz : kz + d.NZH;
+        const float2 v = r[c * ls + sw<T>(slot)];
+        float2 o = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+        if (a.mean_split) {
+          const float2 l = mean_term(a, mr, j, kz, i0 + c);
+          o.x = __fadd_rn(o.x, l.x);
+          o.y = __fadd_rn(o.y, l.y);
+        }
+        dst[(size_t)kz * d.NXH + i0 + c] = to_d(o);
       }
     }
-    // Vbar and Obar_y are the (0, 0) modes of v and omega_y: zero whenever
-    // they start zero (Hv, Hg vanish at k = 0).  Then a row-uniform branch
-    // drops their terms: Ubar x om + u x Obar with Ubar = (U, 0, W), Obar =
-    // (Ox, 0, Oz).
-    if (m != 0 && Ub[1] == 0.0 && Ob[1] == 0.0) {
-      // x: -W oy + v Oz ; y: W ox - U oz + w Ox - u Oz ; z: U oy - v Ox
-      a.lm[0][e] = make_double2(F[1].x * Ob[2] - Ub[2] * F[4].x, F[1].y * Ob[2] - Ub[2] * F[4].y);
-      a.lm[1][e] = make_double2(Ub[2] * F[3].x - Ub[0] * F[5].x + F[2].x * Ob[0] - F[0].x * Ob[2],
-                                Ub[2] * F[3].y - Ub[0] * F[5].y + F[2].y * Ob[0] - F[0].y * Ob[2]);
-      a.lm[2][e] = make_double2(Ub[0] * F[4].x - F[1].x * Ob[0], Ub[0] * F[4].y - F[1].y * Ob[0]);
-      return;
-    }
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
-      double2 l;
-      if (m == 0) {
-        l = make_double2(Ub[f1] * Ob[f2] - Ub[f2] * Ob[f1], 0.0);
-      } else {
-        // (a x b)_f = a_f1 b_f2 - a_f2 b_f1
-        const double2 o1 = F[3 + f1], o2 = F[3 + f2], u1 = F[f1], u2 = F[f2];
-        l = make_double2(Ub[f1] * o2.x - Ub[f2] * o1.x + u1.x * Ob[f2] - u2.x * Ob[f1],
-                         Ub[f1] * o2.y - Ub[f2] * o1.y + u1.y * Ob[f2] - u2.y * Ob[f1]);
+  } else {
+    const double sc = a.inv_nz2;
+    for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
+      const int kz = idx / TX, c = idx - kz * TX;
+      if (i0 + c < d.NXH) {
+        const int slot = kz < d.NZH ? kz : kz + d.NZH;
+        const double2 v = r[c * ls + sw<T>(slot)];
+        // explicit roundings: the batched and the one-channel kernels must
+        // give the same bits whatever each compilation contracts
+        dst[(size_t)kz * d.NXH + i0 + c] = make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
       }
-      a.lm[f][e] = l;
     }
   }
 }
@@ -268,9 +208,6 @@ __global__ void __maxnreg__(XCfg<T>::XREG) k_xlamb(const __grid_constant__ Xform
 template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zfwd(const __grid_constant__ XformArgs a) {
   zfwd_body<T, R5>(a, blockIdx.x, blockIdx.y, blockIdx.z);
-}
-__global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ XformArgs a) {
-  mean_lamb_body(a, blockIdx.x, blockIdx.y);
 }
 
 // Stand-alone dealiased transforms of one field in FP64 (the reference's
@@ -359,17 +296,6 @@ __global__ void __launch_bounds__(1024) k_zfwd_batch(const __grid_constant__ Bat
   const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
   zfwd_body<T, R5>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
 }
-__global__ void __launch_bounds__(256) k_mean_lamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
-  const int c = batch_channel(t.start, t.n, blockIdx.x);
-  const XformArgs &a = t.a[c];
-  const int gx = (a.d.NZ * a.d.NXH + 255) / 256, lb = blockIdx.x - t.start[c], r = lb / gx;
-  mean_lamb_body(a, lb - r * gx, r);
-}
-
-static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
-  const int M = a.d.NZ * a.d.NXH;
-  k_mean_lamb<<<dim3((M + 255) / 256, a.d.NY), 256, 0, st>>>(a);
-}
 
 template <typename T>
 static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * line_stride<T>(d.NZ2) * sizeof(cpx<T>); }
@@ -437,8 +363,7 @@ static XformKernels<T> kernels(const XformDims &d, bool stockham = false) {
   return k;
 }
 
-// One of the kernels (0: z backward, 1: x pass, 2: z forward, 3: the
-// mean-flow term of the mixed-precision Lamb vector).
+// One of the kernels (0: z backward, 1: x pass, 2: z forward).
 template <typename T>
 static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   const XformDims &d = a.d;
@@ -453,18 +378,12 @@ static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
     k.xlamb<<<(unsigned)grid, k.xthreads, k.xsmem, st>>>(a);
   } else if (part == 2) {
     k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), k.zthreads, k.zsmem, st>>>(a);
-  } else if (a.mean_split) {
-    launch_mean_lamb(a, st);
   }
 }
-
-// On one stream: the mean-flow terms (mixed precision) first, as the z
-// forward adds them.
 template <typename T>
 static int lamb_t(const XformArgs &a, cudaStream_t st) {
-  if (a.mean_split) lamb_part_t<T>(a, 3, st);
   for (int part = 0; part < 3; ++part) lamb_part_t<T>(a, part, st);
-  return a.mean_split ? 4 : 3;
+  return 3;
 }
 
 // Opt the channel's transform kernels (single and batched) in to the dynamic
@@ -498,18 +417,15 @@ void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t 
   else lamb_part_t<float>(a, part, st);
 }
 
-// Blocks of one channel in part 0 (z backward), 1 (x pass), 2 (z forward) or
-// 3 (mean-flow terms); the grids of the one-channel launches, flattened.
+// Blocks of one channel in part 0 (z backward), 1 (x pass) or 2 (z forward);
+// the grids of the one-channel launches, flattened.
 template <typename T>
 static int lamb_blocks_t(const XformDims &d, int part, bool stockham) {
   const int gx = (d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX;
   if (part == 0) return gx * d.NY * 6;
   if (part == 2) return gx * d.NY * 3;
-  if (part == 1) {
-    const int P = kernels<T>(d, stockham).P;
-    return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
-  }
-  return ((d.NZ * d.NXH + 255) / 256) * d.NY;
+  const int P = kernels<T>(d, stockham).P;
+  return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
 }
 int lamb_batch_blocks(const XformDims &d, int precision, int part, bool stockham) {
   return precision == 0 ? lamb_blocks_t<double>(d, part, stockham) : lamb_blocks_t<float>(d, part, stockham);
@@ -527,8 +443,7 @@ static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t 
   if (part == 0) k.zback_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
   else if (part == 1) k.xlamb_b<<<k.xgrid > 0 && blocks > (unsigned)k.xgrid ? (unsigned)k.xgrid : blocks, k.xthreads,
                                   k.xsmem, st>>>(t);
-  else if (part == 2) k.zfwd_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
-  else k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
+  else k.zfwd_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
 }
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_batch_t<double>(t, part, st);
@@ -574,6 +489,84 @@ size_t lamb_zbuf_bytes(const XformDims &d, int precision) {
 }
 size_t lamb_lbuf_bytes(const XformDims &d, int precision) {
   return 3 * (size_t)d.NY * d.NZ2 * d.NXH * (precision == 0 ? sizeof(double2) : sizeof(float2));
+}
+
+// ---------------------------------------------------------------------------
+// Check of d2f_bits / f2d_bits against the hardware conversions.  Sample i
+// is one of the edge values below (i < kConvEdges) or a splitmix64 bit
+// pattern: doubles with exponents across the FP32 range and a little beyond,
+// floats of every exponent.  counts: [0] d2f results equal to
+// __double2float_rn, [1] d2f ties (the dropped bits exactly half an ulp)
+// rounded away from zero where the hardware rounds to even, [2] d2f
+// subnormal results flushed to zero, [3] d2f results outside these three,
+// [4] f2d results equal to the hardware's (NaN as NaN), [5] FP32 subnormals
+// widened to a signed zero, [6] f2d results outside these two.
+// ---------------------------------------------------------------------------
+constexpr int kConvEdges = 16;
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ bool f_is_nan(float f) { return (__float_as_uint(f) & 0x7fffffffu) > 0x7f800000u; }
+
+__global__ void k_convert_check(long long n, uint64_t seed, unsigned long long *counts) {
+  unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t r = splitmix64(seed ^ (uint64_t)i * 0x2545f4914f6cdd1dull), r2 = splitmix64(r);
+    double x;
+    if (i < kConvEdges) {
+      // 0, -0, inf, -inf, NaN, ties with an even and an odd kept bit, the
+      // largest float, 2^128 (overflow), just below the rounding-to-2^128
+      // boundary, the smallest normal, half of it, 1, -1, 1/3, 1e30
+      const uint64_t e[kConvEdges] = {0x0000000000000000ull, 0x8000000000000000ull, 0x7ff0000000000000ull,
+                                      0xfff0000000000000ull, 0x7ff8000000000001ull, 0x3ff0000010000000ull,
+                                      0x3ff0000030000000ull, 0x47efffffe0000000ull, 0x47f0000000000000ull,
+                                      0x47efffffefffffffull, 0x3810000000000000ull, 0x3800000000000000ull,
+                                      0x3ff0000000000000ull, 0xbff0000000000000ull, 0x3fd5555555555555ull,
+                                      0x46293e5939a08ceaull};
+      x = __longlong_as_double((long long)e[i]);
+    } else {
+      // exponent 1023 + [-140, 140), random sign and fraction
+      const uint64_t ex = (uint64_t)(1023 - 140 + (int)(r2 % 280));
+      x = __longlong_as_double((long long)((r & 0x800fffffffffffffull) | (ex << 52)));
+    }
+    const float got = d2f_bits(x), want = __double2float_rn(x);
+    const unsigned ug = __float_as_uint(got), uw = __float_as_uint(want);
+    const unsigned lo = (unsigned)__double2loint(x), ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    const bool tie = (lo & 0x1fffffffu) == 0x10000000u && ah >= (897u << 20) && ah < (1151u << 20);
+    if (ug == uw || (f_is_nan(got) && f_is_nan(want))) ++c[0];
+    else if (tie && (ug & 0x7fffffffu) == (uw & 0x7fffffffu) + 1u && (ug >> 31) == (uw >> 31)) ++c[1];
+    else if ((ug & 0x7fffffffu) == 0u && (uw & 0x7fffffffu) <= 0x00800000u && (ug >> 31) == (uw >> 31)) ++c[2];
+    else ++c[3];
+    // floats: every bit pattern is a candidate
+    const float f = __uint_as_float((unsigned)(r2 >> 32));
+    const double gd = f2d_bits(f), wd = (double)f;
+    const unsigned long long bg = (unsigned long long)__double_as_longlong(gd),
+                             bw = (unsigned long long)__double_as_longlong(wd);
+    const unsigned af = __float_as_uint(f) & 0x7fffffffu;
+    if (bg == bw || (gd != gd && wd != wd)) ++c[4];
+    else if (af != 0u && af < 0x00800000u && (bg & 0x7fffffffffffffffull) == 0ull && (bg >> 63) == (bw >> 63)) ++c[5];
+    else ++c[6];
+  }
+  for (int k = 0; k < 7; ++k)
+    if (c[k]) atomicAdd(counts + k, c[k]);
+}
+
+int convert_selftest(long long n, uint64_t seed, long long counts[7]) {
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 7 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    k_convert_check<<<1024, 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[7] = {};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  for (int k = 0; k < 7; ++k) counts[k] = (long long)h[k];
+  return e == cudaSuccess ? 0 : 1;
 }
 
 }  // namespace owt

@@ -56,6 +56,7 @@ def load(path=LIB):
         "owt_init_seeded": ([_h, C.c_uint64, C.c_double], C.c_int),
         "owt_band_factor_selftest": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_int64),
                                       C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+        "owt_convert_selftest": ([C.c_int64, C.c_uint64, C.POINTER(C.c_int64)], C.c_int),
         "owt_time_integration": ([_h, C.c_int64], C.c_int),
         "owt_call": ([_h, C.c_int], C.c_int),
         "owt_synchronize": ([_h], C.c_int),

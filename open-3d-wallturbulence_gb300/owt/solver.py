@@ -229,9 +229,9 @@ class GpuSolver:
         self._chk(self.L.owt_set_option(self.h, 3, 1 if on else 0))
 
     def use_mean_split(self, on=True):
-        """Mixed precision: FP64 mean-flow terms of the Lamb vector beside the
-        FP32 transforms (the default), or the whole fields through FP32
-        (OWT_OPT_MEAN_SPLIT)."""
+        """Mixed precision: the mean-flow terms of the Lamb vector formed mode by
+        mode beside the FP32 transforms of the fluctuations (the default), or
+        the whole fields through FP32 (OWT_OPT_MEAN_SPLIT)."""
         self._chk(self.L.owt_set_option(self.h, 4, 1 if on else 0))
 
     def set_host_chunks(self, n):
