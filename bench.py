@@ -281,7 +281,7 @@ def run_ours(args, rank, world, local_rank):
                 solver.synchronize()
                 out[name] = e0.elapsed_time(e1) / reps
 
-        time_stages("mixed", (("zback", 4), ("xlamb", 5), ("zfwd", 6)), stage_ms_mixed)
+        time_stages("mixed", (("zback", 4), ("xlamb", 5), ("zfwd", 6), ("mean_lamb", 7)), stage_ms_mixed)
         time_stages(args.precision, (("modes", 0), ("zback", 4), ("xlamb", 5), ("zfwd", 6), ("nonlinear", 3)),
                     stage_ms)
 

@@ -268,8 +268,9 @@ int owt_state_restore(owt_handle *h);
  * OWT_OPT_MEAN_SPLIT: mixed precision only; 1 (the default) = the FP32
  *   transforms carry the fluctuations, and the mean-flow terms of the Lamb
  *   vector (mean velocity x fluctuating vorticity and back) are formed mode
- *   by mode by the z forward transform, each with an FP32 rounding of its own
- *   size; 0 = the FP32 transforms carry the whole fields.
+ *   by mode beside them in FP32, each with a rounding of its own size (not of
+ *   the largest value of a transformed plane); 0 = the FP32 transforms carry
+ *   the whole fields.
  * OWT_OPT_HOST_CHUNKS: owt_time_integration_host pipelines its uploads with
  *   the mode kernel over this many chunks of Fourier modes (1 .. 8; 0 = the
  *   default, 2) when the mode kernel in use maps threads by quads.
@@ -306,14 +307,12 @@ const char *owt_setup_report(const owt_handle *h);
 int owt_band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, int64_t *mismatches, float *ms_thread,
                              float *ms_warp);
 
-/* Testing aid, no counterpart in the reference: the FP64 <-> FP32
- * conversions of the mixed precision's transforms (integer instructions,
- * instead of the hardware conversions on the FP64 pipe) against the
- * hardware's, on n samples (edge values, then seeded random bit patterns).
- * counts[7]: FP64 -> FP32 results equal to the hardware's round to nearest
- * even; ties rounded away from zero instead; subnormal results flushed to
- * zero; any other result; FP32 -> FP64 results equal to the hardware's;
- * FP32 subnormals widened to zero; any other result. */
+/* Testing aid, no counterpart in the reference: the FP64 -> FP32 conversion
+ * of the mixed precision's mean-flow terms (integer instructions, instead of
+ * the hardware conversion on the FP64 pipe) against the hardware's, on n
+ * samples (edge values, then seeded random bit patterns).  counts[4]: results
+ * equal to the hardware's round to nearest even; ties rounded away from zero
+ * instead; subnormal results flushed to zero; any other result. */
 int owt_convert_selftest(int64_t n, uint64_t seed, int64_t *counts);
 
 /* Measurement aid, no counterpart in the reference: enqueue one stage of the
@@ -325,7 +324,9 @@ int owt_convert_selftest(int64_t n, uint64_t seed, int64_t *counts);
  *   2: transforms + products (Lamb vector, three kernels)
  *   3: nonlinear source
  *   4, 5, 6: the three transform kernels alone (z backward, x pass with the
- *            products, z forward with the mixed precision's mean-flow terms) */
+ *            products, z forward)
+ *   7: the mean-flow terms of the mixed-precision Lamb vector (FP32, mode by
+ *      mode; nothing in FP64) */
 #define OWT_STAGE_MODES 0
 #define OWT_STAGE_MEAN 1
 #define OWT_STAGE_LAMB 2
@@ -333,6 +334,7 @@ int owt_convert_selftest(int64_t n, uint64_t seed, int64_t *counts);
 #define OWT_STAGE_ZBACK 4
 #define OWT_STAGE_XLAMB 5
 #define OWT_STAGE_ZFWD 6
+#define OWT_STAGE_MEAN_LAMB 7 /* mixed precision: the mean-flow terms of the Lamb vector */
 int owt_enqueue_stage(owt_handle *h, int stage);
 
 /* Wall blowing/suction.  The reference imposes v = 0 on both walls through

@@ -75,13 +75,13 @@ int owt_convert_selftest(int64_t n, uint64_t seed, int64_t *counts) {
     g_create_error = "owt_convert_selftest: bad arguments";
     return OWT_ERR_INVALID;
   }
-  long long c[7] = {};
+  long long c[4] = {};
   if (convert_selftest(n, seed, c) != 0) {
     g_create_error = "owt_convert_selftest: CUDA error";
     cudaGetLastError();
     return OWT_ERR_CUDA;
   }
-  for (int k = 0; k < 7; ++k) counts[k] = c[k];
+  for (int k = 0; k < 4; ++k) counts[k] = c[k];
   return OWT_OK;
 }
 
@@ -291,7 +291,7 @@ int owt_enqueue_stage(owt_handle *h, int stage) {
       case OWT_STAGE_MEAN: h->stage_mean(); h->launches += 1; break;
       case OWT_STAGE_LAMB: h->launches += launch_lamb(h->xform_args(), h->precision, h->st); break;
       case OWT_STAGE_NONLINEAR: launch_nl(h->nl_args(true), h->st); h->launches += 1; break;
-      case OWT_STAGE_ZBACK: case OWT_STAGE_XLAMB: case OWT_STAGE_ZFWD:
+      case OWT_STAGE_ZBACK: case OWT_STAGE_XLAMB: case OWT_STAGE_ZFWD: case OWT_STAGE_MEAN_LAMB:
         launch_lamb_part(h->xform_args(), h->precision, stage - OWT_STAGE_ZBACK, h->st);
         h->launches += 1;
         break;

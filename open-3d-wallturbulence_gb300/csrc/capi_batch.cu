@@ -40,6 +40,7 @@ struct owt_batch {
   std::vector<owt_handle *> hs;
   cudaStream_t st = nullptr, st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;    // the mean mode beside the mode kernel
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;  // the mean-flow terms beside the transforms
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int *work = nullptr;        // counter pairs of the persistent mode launches
@@ -68,7 +69,7 @@ struct owt_batch {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (work) cudaFree(work);
-    for (cudaEvent_t e : {ev_fork, ev_join})
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
       if (e) cudaEventDestroy(e);
     if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
@@ -133,16 +134,17 @@ struct owt_batch {
     // transforms: grouped by precision and the line length of the kernel
     std::vector<XformArgs> xargs;
     for (owt_handle *h : hs) xargs.push_back(h->xform_args());
-    for (int part = 0; part < 3; ++part) {
+    for (int part = 0; part < 4; ++part) {
       std::map<std::tuple<int, int, int>, std::vector<int>> groups;  // (precision, line length, Stockham kernels)
       std::vector<int> blocks(n, 0);
       for (int i = 0; i < n; ++i) {
         const owt_handle *h = hs[i];
+        if (part == 3 && !xargs[i].mean_split) continue;
         const XformDims &d = xargs[i].d;
         const int prec = h->precision == OWT_PREC_MIXED ? 1 : 0;
         if (part == 0) ck(lamb_batch_prepare(d, prec), "transform kernel attributes");
         blocks[i] = lamb_batch_blocks(d, prec, part, xargs[i].stockham != 0);
-        const int len = part == 1 ? d.NX2 : d.NZ2;
+        const int len = part == 1 ? d.NX2 : part == 3 ? 0 : d.NZ2;
         groups[std::make_tuple(prec, len, xargs[i].stockham)].push_back(i);
       }
       for (auto &g : groups)
@@ -177,9 +179,22 @@ struct owt_batch {
       launch_advance_batch(c, st);
       ++step_launches;
     }
-    for (auto &l : lamb) {
-      launch_lamb_batch(*l.t, l.precision, l.part, st);
-      ++step_launches;
+    // the mean-flow terms of the mixed-precision channels beside the z
+    // backward and x pass; the z forward adds them
+    bool split = false;
+    for (auto &l : lamb) split = split || l.part == 3;
+    if (split) {
+      ck(cudaEventRecord(ev_fork2, st), "fork");
+      ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
+    }
+    for (int part : {3, 0, 1, 2}) {
+      if (part == 2 && split) ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
+      for (auto &l : lamb)
+        if (l.part == part) {
+          launch_lamb_batch(*l.t, l.precision, l.part, part == 3 ? st2 : st);
+          ++step_launches;
+        }
+      if (part == 3 && split) ck(cudaEventRecord(ev_join2, st2), "join");
     }
     for (auto &t : nl) {
       launch_nl_batch(*t, st);
@@ -289,6 +304,8 @@ int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
     ck(cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_fork2, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming), "event");
     const size_t n_mode_tables = (b->by_size(true).size() + kBatchChannels - 1) / kBatchChannels +
                                  (b->by_size(false).size() + kBatchChannels - 1) / kBatchChannels;
     ck(cudaMalloc(&b->work, 2 * n_mode_tables * sizeof(int)), "work counters");

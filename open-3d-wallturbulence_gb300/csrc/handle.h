@@ -87,6 +87,7 @@ struct owt_handle {
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;                    // the mean-mode branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;    // the mean mode beside the mode kernel
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;  // the mean-flow terms beside the transforms
   std::vector<void *> owned;
   int64_t steps = 0;
   int64_t launches = 0;
@@ -109,6 +110,7 @@ struct owt_handle {
   double2 *u = nullptr, *w = nullptr, *ox = nullptr, *oz = nullptr, *lx = nullptr, *ly = nullptr, *lz = nullptr;
   double2 *U_ring = nullptr, *W_ring = nullptr, *lxm_ring = nullptr, *lzm_ring = nullptr;
   double *fx_ring = nullptr, *fz_ring = nullptr;
+  float2 *lm = nullptr;  // mixed precision: the mean-flow terms of the Lamb vector [3][NY][M], FP32
   double *ygrid = nullptr, *wy = nullptr;  // y and its trapezoidal weights (summing to 1)
   double *ic_partial = nullptr;            // seeded initial condition: RMS partial sums
   long long *d_step = nullptr;
@@ -171,7 +173,7 @@ struct owt_handle {
   int64_t per_step_launches = 0;
   bool force_dense = false;  // testing aid: always sweep the full band
   bool fft_stockham = false; // FP32 transforms: shared-memory Stockham kernels instead of register ones
-  bool mean_split = true;    // mixed precision: the mean-flow terms of the Lamb vector mode by mode, not transformed
+  bool mean_split = true;    // mixed precision: the mean-flow terms of the Lamb vector mode by mode beside the transforms
   int host_chunks = 0;       // owt_time_integration_host: chunks of modes (0: the default)
   bool mean_smem = false;    // staged mean-mode solve in shared memory
   int modes_variant = 0;     // chosen by the autotuner

@@ -15,7 +15,7 @@ owt_handle::~owt_handle() {
   if (gexec) cudaGraphExecDestroy(gexec);
   if (graph) cudaGraphDestroy(graph);
   for (void *q : owned) cudaFree(q);
-  for (cudaEvent_t e : {ev_fork, ev_join})
+  for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2})
     if (e) cudaEventDestroy(e);
   if (hs.ready) {
     for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamSynchronize(q);
@@ -76,6 +76,8 @@ void owt_handle::setup(const owt_params &prm) {
   ck(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
   ck(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
   ck(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  ck(cudaEventCreateWithFlags(&ev_fork2, cudaEventDisableTiming), "cudaEventCreate");
+  ck(cudaEventCreateWithFlags(&ev_join2, cudaEventDisableTiming), "cudaEventCreate");
 
   // grid, metric, stencils, band templates (host, FP64)
   grid = make_grid(NY, p.alpha_mesh);
@@ -227,6 +229,7 @@ void owt_handle::setup(const owt_params &prm) {
   q_ring = dalloc<double2>(3 * fs, owned);
   for (double2 **f : {&u, &w, &ox, &oz, &lx, &ly, &lz, &sg, &dg, &sv, &bf, &yscr, &tmpA, &tmpB, &tmpC, &stage})
     *f = dalloc<double2>(fs, owned);
+  lm = dalloc<float2>(3 * fs, owned);
   {
     std::vector<double> wyh(NY, 0.0);
     double tot = 0.0;

@@ -26,6 +26,7 @@ XformArgs owt_handle::xform_args() const {
   a.fs = fs;
   a.step = d_step;
   a.mean_split = (precision == OWT_PREC_MIXED && mean_split) ? 1 : 0;
+  for (int f = 0; f < 3; ++f) a.lm[f] = lm + (size_t)f * fs;
   a.out[0] = lx; a.out[1] = ly; a.out[2] = lz;
   a.zbuf = zbuf; a.lbuf = lbuf;
   a.px = px; a.pz = pz;
@@ -75,7 +76,22 @@ void owt_handle::step_begin() {
 void owt_handle::step_finish() {
   ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launch_advance(d_step, st);
-  const int nx = launch_lamb(xform_args(), precision, st);
+  const XformArgs xa = xform_args();
+  int nx = 3;
+  if (xa.mean_split) {
+    // the mean-flow terms beside the FP32 z backward and x pass
+    ck(cudaEventRecord(ev_fork2, st), "fork");
+    ck(cudaStreamWaitEvent(st2, ev_fork2, 0), "fork wait");
+    launch_lamb_part(xa, precision, 3, st2);
+    ck(cudaEventRecord(ev_join2, st2), "join");
+    launch_lamb_part(xa, precision, 0, st);
+    launch_lamb_part(xa, precision, 1, st);
+    ck(cudaStreamWaitEvent(st, ev_join2, 0), "join wait");
+    launch_lamb_part(xa, precision, 2, st);
+    nx = 4;
+  } else {
+    nx = launch_lamb(xa, precision, st);
+  }
   launch_nl(nl_args(true), st);
   launches += 4 + nx;
 }

@@ -1,5 +1,6 @@
 // Mixed precision: the interaction of the mean flow with the fluctuations,
-// added to the Lamb vector by the FP32 z forward kernels element by element.
+// formed mode by mode beside the FP32 transforms (k_mean_lamb) and added to
+// the Lamb vector by the z forward kernels.
 //
 // With the mean split on, the z backward leaves mode (0, 0) of every field
 // out of the FP32 transforms, so the product the transforms form is the
@@ -28,56 +29,69 @@ __device__ __forceinline__ const double2 *xform_field_row(const XformArgs &a, in
   return base + (size_t)j * a.d.NZ * a.d.NXH;
 }
 
-// The mean profiles component f of row j needs: with f1 = f + 1, f2 = f + 2
-// (mod 3), Ubar_f1, Ubar_f2, Obar_f1, Obar_f2 in FP32.
-struct MeanRow {
-  int f1, f2;
-  float u1, u2, o1, o2;
-};
-
-__device__ __forceinline__ MeanRow mean_row(const XformArgs &a, int j, int f) {
-  MeanRow r;
-  r.f1 = f == 2 ? 0 : f + 1;
-  r.f2 = f == 0 ? 2 : f - 1;
-  r.u1 = d2f_bits(xform_field_row(a, r.f1, j)[0].x);
-  r.u2 = d2f_bits(xform_field_row(a, r.f2, j)[0].x);
-  r.o1 = d2f_bits(xform_field_row(a, 3 + r.f1, j)[0].x);
-  r.o2 = d2f_bits(xform_field_row(a, 3 + r.f2, j)[0].x);
-  return r;
-}
-
-// Component f (that of mean_row) of the mean-flow terms at mode (kz, kx) of
-// row j.  A term whose mean-profile factor is zero (Vbar and Obar_y always
-// are when they start zero, and every profile on a wall row) is skipped with
-// its load.
-__device__ __forceinline__ float2 mean_term(const XformArgs &a, const MeanRow &r, int j, int kz, int kx) {
+// One thread per mode m of row j (the grid's y; 256-thread blocks along the
+// modes), all three components.  Every value is read once and converted by
+// d2f_bits (this kernel runs beside the FP32 z backward, whose hardware
+// conversions occupy the FP64 pipe); products and sums are explicit FP32
+// roundings, so the batched and one-channel kernels give the same bits.
+__device__ __forceinline__ void mean_lamb_body(const XformArgs &a, const int bx, const int j) {
   const XformDims d = a.d;
-  if (kz == d.NZH) return make_float2(0.f, 0.f);
-  if (kz == 0 && kx == 0) return make_float2(__fsub_rn(__fmul_rn(r.u1, r.o2), __fmul_rn(r.u2, r.o1)), 0.f);
-  const size_t at = (size_t)kz * d.NXH + kx;
-  const size_t mirror = (size_t)(kz == 0 ? 0 : d.NZ - kz) * d.NXH;
-  auto F = [&](int q) -> float2 {
-    const double2 *row = xform_field_row(a, q, j);
-    const double2 x = row[at];
-    if (kx != 0) return make_float2(d2f_bits(x.x), d2f_bits(x.y));
-    const double2 y = row[mirror];
-    return make_float2(__fmul_rn(0.5f, __fadd_rn(d2f_bits(x.x), d2f_bits(y.x))),
-                       __fmul_rn(0.5f, __fsub_rn(d2f_bits(x.y), d2f_bits(y.y))));
-  };
+  const int M = d.NZ * d.NXH;
+  const int m = bx * 256 + threadIdx.x;
+  if (m >= M) return;
+  const int kz = m / d.NXH, kx = m - kz * d.NXH;
+  const size_t e = (size_t)j * M + m;
+  if (kz == d.NZH) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) a.lm[f][e] = make_float2(0.f, 0.f);
+    return;
+  }
+  const double2 *row[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) row[q] = xform_field_row(a, q, j);
+  float Ub[3], Ob[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    Ub[q] = d2f_bits(row[q][0].x);
+    Ob[q] = d2f_bits(row[3 + q][0].x);
+  }
+  if (m == 0) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
+      a.lm[f][e] = make_float2(__fsub_rn(__fmul_rn(Ub[f1], Ob[f2]), __fmul_rn(Ub[f2], Ob[f1])), 0.f);
+    }
+    return;
+  }
+  float2 F[6];
+  const int mirror = (kz == 0 ? 0 : d.NZ - kz) * d.NXH;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const double2 x = row[q][m];
+    if (kx != 0) {
+      F[q] = make_float2(d2f_bits(x.x), d2f_bits(x.y));
+    } else {
+      const double2 y = row[q][mirror];
+      F[q] = make_float2(__fmul_rn(0.5f, __fadd_rn(d2f_bits(x.x), d2f_bits(y.x))),
+                         __fmul_rn(0.5f, __fsub_rn(d2f_bits(x.y), d2f_bits(y.y))));
+    }
+  }
   // (a x b)_f = a_f1 b_f2 - a_f2 b_f1, linear part in the fluctuations:
   // Ubar_f1 om_f2 - Ubar_f2 om_f1 + u_f1 Obar_f2 - u_f2 Obar_f1
-  float2 acc = make_float2(0.f, 0.f);
-  auto add = [&](float c, int q) {
-    if (c == 0.f) return;
-    const float2 v = F(q);
-    acc.x = __fmaf_rn(c, v.x, acc.x);
-    acc.y = __fmaf_rn(c, v.y, acc.y);
-  };
-  add(r.u1, 3 + r.f2);
-  add(-r.u2, 3 + r.f1);
-  add(r.o2, r.f1);
-  add(-r.o1, r.f2);
-  return acc;
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const int f1 = (f + 1) % 3, f2 = (f + 2) % 3;
+    float2 acc;
+    acc.x = __fmul_rn(Ub[f1], F[3 + f2].x);
+    acc.y = __fmul_rn(Ub[f1], F[3 + f2].y);
+    acc.x = __fmaf_rn(-Ub[f2], F[3 + f1].x, acc.x);
+    acc.y = __fmaf_rn(-Ub[f2], F[3 + f1].y, acc.y);
+    acc.x = __fmaf_rn(Ob[f2], F[f1].x, acc.x);
+    acc.y = __fmaf_rn(Ob[f2], F[f1].y, acc.y);
+    acc.x = __fmaf_rn(-Ob[f1], F[f2].x, acc.x);
+    acc.y = __fmaf_rn(-Ob[f1], F[f2].y, acc.y);
+    a.lm[f][e] = acc;
+  }
 }
 
 }  // namespace owt

@@ -30,20 +30,17 @@ template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
 
 
 // ---------------------------------------------------------------------------
-// FP64 <-> FP32 conversions in integer instructions.  The hardware
-// conversions run on the FP64 pipe, which on this part executes about two
-// operations a clock per SM: converting the step's fields took half the time
-// of the FP32 z transforms.  These take ten integer operations or fewer, on
-// the integer pipes, from the IEEE-754 bit layouts (binary64: sign, 11-bit
-// exponent biased by 1023, 52-bit fraction; binary32: sign, 8-bit exponent
-// biased by 127, 23-bit fraction):
-//  d2f_bits: round to nearest, ties away from zero (the hardware's
-//    round-to-nearest-even differs only when the 29 dropped fraction bits
-//    are exactly 1 followed by zeros); magnitudes below 2^-126 (the smallest
-//    FP32 normal) become a signed zero; magnitudes at or above 2^128, and
-//    those that round up to it, become infinity; NaN stays NaN.
-//  f2d_bits: exact for zero and every FP32 normal; FP32 subnormals become a
-//    signed zero; infinities and NaN are kept.
+// FP64 -> FP32 conversion in integer instructions, for kernels that convert
+// many values beside other kernels' hardware conversions: those run on the
+// FP64 pipe, which on this part executes about two operations a clock per
+// SM.  Ten integer operations or fewer, from the IEEE-754 bit layouts
+// (binary64: sign, 11-bit exponent biased by 1023, 52-bit fraction; binary32:
+// sign, 8-bit exponent biased by 127, 23-bit fraction): round to nearest,
+// ties away from zero (the hardware's round-to-nearest-even differs only
+// when the 29 dropped fraction bits are exactly 1 followed by zeros);
+// magnitudes below 2^-126 (the smallest FP32 normal) become a signed zero;
+// magnitudes at or above 2^128, and those that round up to it, become
+// infinity; NaN stays NaN.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float d2f_bits(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
@@ -56,20 +53,13 @@ __device__ __forceinline__ float d2f_bits(double x) {
   if (ah >= (1151u << 20)) m = (ah > 0x7ff00000u || (ah == 0x7ff00000u && lo)) ? 0x7fc00000u : 0x7f800000u;
   return __uint_as_float(m | (hi & 0x80000000u));
 }
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned u = __float_as_uint(f), au = u & 0x7fffffffu, sg = u & 0x80000000u;
-  unsigned hi = ((au >> 3) + (896u << 20)) | sg, lo = au << 29;
-  if (au < 0x00800000u) hi = sg, lo = 0u;
-  if (au >= 0x7f800000u) hi = sg | 0x7ff00000u | ((au & 0x007fffffu) ? 0x00080000u : 0u), lo = 0u;
-  return __hiloint2double((int)hi, (int)lo);
-}
 
 // Complex values between the FP64 state and the FP32 transforms.
 __device__ __forceinline__ double2 to_d(double2 a) { return a; }
-__device__ __forceinline__ double2 to_d(float2 a) { return make_double2(f2d_bits(a.x), f2d_bits(a.y)); }
+__device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
 template <typename T> __device__ __forceinline__ cpx<T> from_d(double2 a);
 template <> __device__ __forceinline__ double2 from_d<double>(double2 a) { return a; }
-template <> __device__ __forceinline__ float2 from_d<float>(double2 a) { return make_float2(d2f_bits(a.x), d2f_bits(a.y)); }
+template <> __device__ __forceinline__ float2 from_d<float>(double2 a) { return make_float2((float)a.x, (float)a.y); }
 
 // ---------------------------------------------------------------------------
 // FFT of many lines held in shared memory: self-sorting (Stockham) mixed-radix

@@ -120,9 +120,10 @@ struct XformArgs {
   size_t fs;
   const long long *step;
   // mixed precision (FP32 transforms only): transform only the fluctuations
-  // (mode (0,0) left out); the z forward adds the mean-flow interaction
-  // terms mode by mode (mean_flow.cuh)
+  // (mode (0,0) left out); k_mean_lamb writes the mean-flow interaction terms
+  // (formed mode by mode, mean_flow.cuh) to lm and the z forward adds them
   int mean_split;
+  float2 *lm[3];  // [NY][M] each
   double2 *out[3];
   void *zbuf;  // [6][NY][NZ2][NXH] complex<T>
   void *lbuf;  // [3][NY][NZ2][NXH] complex<T>
@@ -133,9 +134,9 @@ struct XformArgs {
 };
 
 bool band_supported(int kl, int ku);
-// d2f_bits / f2d_bits against the hardware conversions on n samples (counts:
-// see k_convert_check); 0 on success.
-int convert_selftest(long long n, uint64_t seed, long long counts[7]);
+// d2f_bits against the hardware conversion on n samples (counts: see
+// k_convert_check); 0 on success.
+int convert_selftest(long long n, uint64_t seed, long long counts[4]);
 int band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, long long *mismatches, float *ms_thread,
                          float *ms_warp);
 // Band LU of U systems (dgbtf2 order, row equilibration when rscale is given).

@@ -16,8 +16,9 @@
 //  k_zfwd  : per (y, kx tile, field) -- forward FFT of length NZ2, keep slots
 //            k < NZH and NZ + k (k < NZH) -> kz index k + NZH, / NZ2
 //            (FFT.cpp:177-188).  The Nyquist row is kept on this path.
-//            FP32 (mixed precision): plus the mean-flow terms the FP32
-//            transforms leave out, element by element (mean_flow.cuh).
+//            FP32 (mixed precision): plus the mean-flow terms.
+//  k_mean_lamb (mixed precision only): the mean-flow terms that the FP32
+//            transforms leave out, mode by mode in FP32 (mean_flow.cuh).
 //
 // Between kernels the z-padded, x-truncated planes live in HBM as
 // [field][y][z][kx] complex<T>.  T = double (FP64 step) or float (mixed).
@@ -161,22 +162,22 @@ __device__ __forceinline__ void zfwd_body(const XformArgs &a, const int bx, cons
   double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH;
   if constexpr (sizeof(T) == sizeof(float)) {
     // FP32 transforms: the 1/NZ2 normalisation and (mean split) the
-    // mean-flow terms of mean_flow.cuh in FP32, then the exact widening
+    // mean-flow terms k_mean_lamb wrote, in FP32, then the exact widening
     const float sc = (float)a.inv_nz2;
-    MeanRow mr;
-    if (a.mean_split) mr = mean_row(a, j, f);
+    const float2 *lm = a.mean_split ? a.lm[f] + (size_t)j * d.NZ * d.NXH : nullptr;
     for (int idx = threadIdx.x; idx < d.NZ * TX; idx += blockDim.x) {
       const int kz = idx / TX, c = idx - kz * TX;
       if (i0 + c < d.NXH) {
         const int slot = kz < d.NZH ? kz : kz + d.NZH;
         const float2 v = r[c * ls + sw<T>(slot)];
+        const size_t at = (size_t)kz * d.NXH + i0 + c;
         float2 o = make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
-        if (a.mean_split) {
-          const float2 l = mean_term(a, mr, j, kz, i0 + c);
+        if (lm) {
+          const float2 l = lm[at];
           o.x = __fadd_rn(o.x, l.x);
           o.y = __fadd_rn(o.y, l.y);
         }
-        dst[(size_t)kz * d.NXH + i0 + c] = to_d(o);
+        dst[at] = to_d(o);
       }
     }
   } else {
@@ -208,6 +209,9 @@ __global__ void __maxnreg__(XCfg<T>::XREG) k_xlamb(const __grid_constant__ Xform
 template <typename T, bool R5>
 __global__ void __launch_bounds__(1024) k_zfwd(const __grid_constant__ XformArgs a) {
   zfwd_body<T, R5>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+__global__ void __launch_bounds__(256) k_mean_lamb(const __grid_constant__ XformArgs a) {
+  mean_lamb_body(a, blockIdx.x, blockIdx.y);
 }
 
 // Stand-alone dealiased transforms of one field in FP64 (the reference's
@@ -296,6 +300,17 @@ __global__ void __launch_bounds__(1024) k_zfwd_batch(const __grid_constant__ Bat
   const int gx = (a.d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX, lb = blockIdx.x - t.start[c], r = lb / gx;
   zfwd_body<T, R5>(a, lb - r * gx, r % a.d.NY, r / a.d.NY);
 }
+__global__ void __launch_bounds__(256) k_mean_lamb_batch(const __grid_constant__ BatchTable<XformArgs> t) {
+  const int c = batch_channel(t.start, t.n, blockIdx.x);
+  const XformArgs &a = t.a[c];
+  const int gx = (a.d.NZ * a.d.NXH + 255) / 256, lb = blockIdx.x - t.start[c], r = lb / gx;
+  mean_lamb_body(a, lb - r * gx, r);
+}
+
+static void launch_mean_lamb(const XformArgs &a, cudaStream_t st) {
+  const int M = a.d.NZ * a.d.NXH;
+  k_mean_lamb<<<dim3((M + 255) / 256, a.d.NY), 256, 0, st>>>(a);
+}
 
 template <typename T>
 static size_t smem_z(const XformDims &d) { return 2 * (size_t)XCfg<T>::TX * line_stride<T>(d.NZ2) * sizeof(cpx<T>); }
@@ -363,7 +378,8 @@ static XformKernels<T> kernels(const XformDims &d, bool stockham = false) {
   return k;
 }
 
-// One of the kernels (0: z backward, 1: x pass, 2: z forward).
+// One of the kernels (0: z backward, 1: x pass, 2: z forward, 3: the
+// mean-flow terms of the mixed-precision Lamb vector).
 template <typename T>
 static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
   const XformDims &d = a.d;
@@ -378,12 +394,18 @@ static void lamb_part_t(const XformArgs &a, int part, cudaStream_t st) {
     k.xlamb<<<(unsigned)grid, k.xthreads, k.xsmem, st>>>(a);
   } else if (part == 2) {
     k.zfwd<<<dim3((d.NXH + TX - 1) / TX, d.NY, 3), k.zthreads, k.zsmem, st>>>(a);
+  } else if (a.mean_split) {
+    launch_mean_lamb(a, st);
   }
 }
+
+// On one stream: the mean-flow terms (mixed precision) first, as the z
+// forward adds them.
 template <typename T>
 static int lamb_t(const XformArgs &a, cudaStream_t st) {
+  if (a.mean_split) lamb_part_t<T>(a, 3, st);
   for (int part = 0; part < 3; ++part) lamb_part_t<T>(a, part, st);
-  return 3;
+  return a.mean_split ? 4 : 3;
 }
 
 // Opt the channel's transform kernels (single and batched) in to the dynamic
@@ -417,15 +439,18 @@ void launch_lamb_part(const XformArgs &a, int precision, int part, cudaStream_t 
   else lamb_part_t<float>(a, part, st);
 }
 
-// Blocks of one channel in part 0 (z backward), 1 (x pass) or 2 (z forward);
-// the grids of the one-channel launches, flattened.
+// Blocks of one channel in part 0 (z backward), 1 (x pass), 2 (z forward) or
+// 3 (mean-flow terms); the grids of the one-channel launches, flattened.
 template <typename T>
 static int lamb_blocks_t(const XformDims &d, int part, bool stockham) {
   const int gx = (d.NXH + XCfg<T>::TX - 1) / XCfg<T>::TX;
   if (part == 0) return gx * d.NY * 6;
   if (part == 2) return gx * d.NY * 3;
-  const int P = kernels<T>(d, stockham).P;
-  return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
+  if (part == 1) {
+    const int P = kernels<T>(d, stockham).P;
+    return (int)(((size_t)d.NY * d.NZ2 + P - 1) / P);
+  }
+  return ((d.NZ * d.NXH + 255) / 256) * d.NY;
 }
 int lamb_batch_blocks(const XformDims &d, int precision, int part, bool stockham) {
   return precision == 0 ? lamb_blocks_t<double>(d, part, stockham) : lamb_blocks_t<float>(d, part, stockham);
@@ -443,7 +468,8 @@ static void lamb_batch_t(const BatchTable<XformArgs> &t, int part, cudaStream_t 
   if (part == 0) k.zback_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
   else if (part == 1) k.xlamb_b<<<k.xgrid > 0 && blocks > (unsigned)k.xgrid ? (unsigned)k.xgrid : blocks, k.xthreads,
                                   k.xsmem, st>>>(t);
-  else k.zfwd_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
+  else if (part == 2) k.zfwd_b<<<blocks, k.zthreads, k.zsmem, st>>>(t);
+  else k_mean_lamb_batch<<<blocks, 256, 0, st>>>(t);
 }
 void launch_lamb_batch(const BatchTable<XformArgs> &t, int precision, int part, cudaStream_t st) {
   if (precision == 0) lamb_batch_t<double>(t, part, st);
@@ -492,15 +518,12 @@ size_t lamb_lbuf_bytes(const XformDims &d, int precision) {
 }
 
 // ---------------------------------------------------------------------------
-// Check of d2f_bits / f2d_bits against the hardware conversions.  Sample i
-// is one of the edge values below (i < kConvEdges) or a splitmix64 bit
-// pattern: doubles with exponents across the FP32 range and a little beyond,
-// floats of every exponent.  counts: [0] d2f results equal to
-// __double2float_rn, [1] d2f ties (the dropped bits exactly half an ulp)
-// rounded away from zero where the hardware rounds to even, [2] d2f
-// subnormal results flushed to zero, [3] d2f results outside these three,
-// [4] f2d results equal to the hardware's (NaN as NaN), [5] FP32 subnormals
-// widened to a signed zero, [6] f2d results outside these two.
+// Check of d2f_bits against the hardware conversion.  Sample i is one of the
+// edge values below (i < kConvEdges) or a splitmix64 bit pattern with an
+// exponent across the FP32 range and a little beyond.  counts: [0] results
+// equal to __double2float_rn, [1] ties (the dropped bits exactly half an
+// ulp) rounded away from zero where the hardware rounds to even, [2]
+// subnormal results flushed to zero, [3] results outside these three.
 // ---------------------------------------------------------------------------
 constexpr int kConvEdges = 16;
 __device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
@@ -512,7 +535,7 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
 __device__ __forceinline__ bool f_is_nan(float f) { return (__float_as_uint(f) & 0x7fffffffu) > 0x7f800000u; }
 
 __global__ void k_convert_check(long long n, uint64_t seed, unsigned long long *counts) {
-  unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
+  unsigned long long c[4] = {0, 0, 0, 0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const uint64_t r = splitmix64(seed ^ (uint64_t)i * 0x2545f4914f6cdd1dull), r2 = splitmix64(r);
     double x;
@@ -540,32 +563,23 @@ __global__ void k_convert_check(long long n, uint64_t seed, unsigned long long *
     else if (tie && (ug & 0x7fffffffu) == (uw & 0x7fffffffu) + 1u && (ug >> 31) == (uw >> 31)) ++c[1];
     else if ((ug & 0x7fffffffu) == 0u && (uw & 0x7fffffffu) <= 0x00800000u && (ug >> 31) == (uw >> 31)) ++c[2];
     else ++c[3];
-    // floats: every bit pattern is a candidate
-    const float f = __uint_as_float((unsigned)(r2 >> 32));
-    const double gd = f2d_bits(f), wd = (double)f;
-    const unsigned long long bg = (unsigned long long)__double_as_longlong(gd),
-                             bw = (unsigned long long)__double_as_longlong(wd);
-    const unsigned af = __float_as_uint(f) & 0x7fffffffu;
-    if (bg == bw || (gd != gd && wd != wd)) ++c[4];
-    else if (af != 0u && af < 0x00800000u && (bg & 0x7fffffffffffffffull) == 0ull && (bg >> 63) == (bw >> 63)) ++c[5];
-    else ++c[6];
   }
-  for (int k = 0; k < 7; ++k)
+  for (int k = 0; k < 4; ++k)
     if (c[k]) atomicAdd(counts + k, c[k]);
 }
 
-int convert_selftest(long long n, uint64_t seed, long long counts[7]) {
+int convert_selftest(long long n, uint64_t seed, long long counts[4]) {
   unsigned long long *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, 7 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
+  cudaError_t e = cudaMalloc(&d, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     k_convert_check<<<1024, 256>>>(n, seed, d);
     e = cudaGetLastError();
   }
-  unsigned long long h[7] = {};
+  unsigned long long h[4] = {};
   if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
   if (d) cudaFree(d);
-  for (int k = 0; k < 7; ++k) counts[k] = (long long)h[k];
+  for (int k = 0; k < 4; ++k) counts[k] = (long long)h[k];
   return e == cudaSuccess ? 0 : 1;
 }
 

@@ -21,12 +21,11 @@
 //              packed forward lines, the real-pair unpack; thread (q, t), t
 //              fastest; the next group's input lines arrive by cp.async.
 //  k_zfwd_r  : as k_zback_r, forward, keeping kz < NZ/2 and the upper slots,
-//              / NZ2, plus the mean-flow terms (mean_flow.cuh).
+//              / NZ2, plus the mixed precision's mean-flow terms.
 #include <cuda_runtime.h>
 
 #include "batch.cuh"
 #include "fft_reg.cuh"
-#include "mean_flow.cuh"
 #include "owt_device.cuh"
 #include "solve_kernels.h"
 
@@ -110,7 +109,7 @@ __device__ __forceinline__ void zback_r_body(const XformArgs &a, const int bx, c
 }
 
 // ---------------------------------------------------------------------------
-// z forward (+ the mean-flow terms, mean_flow.cuh)
+// z forward (+ the mean-flow terms of the mixed precision)
 // ---------------------------------------------------------------------------
 template <int A, int B>
 __device__ __forceinline__ void zfwd_r_body(const XformArgs &a, const int bx, const int j, const int f) {
@@ -141,11 +140,10 @@ __device__ __forceinline__ void zfwd_r_body(const XformArgs &a, const int bx, co
     for (int q = 0; q < B; ++q) y[q] = T0[t * G::RS + q];
     dft<B, false, float>(y);
     double2 *dst = a.out[f] + (size_t)j * d.NZ * d.NXH + i;
-    // the 1/NZ2 normalisation and the mean-flow terms in FP32, then the
-    // exact widening to FP64
+    const float2 *lm = a.mean_split ? a.lm[f] + (size_t)j * d.NZ * d.NXH + i : nullptr;
+    // the 1/NZ2 normalisation and the mean-flow terms k_mean_lamb wrote, in
+    // FP32, then the exact widening
     const float sc = (float)a.inv_nz2;
-    MeanRow mr;
-    if (a.mean_split) mr = mean_row(a, j, f);
 #pragma unroll
     for (int q = 0; q < B; ++q) {
       const int s = t + A * q;  // keep slots k < NZH (kz k) and NZ + k (kz k + NZH)
@@ -154,8 +152,8 @@ __device__ __forceinline__ void zfwd_r_body(const XformArgs &a, const int bx, co
       else if (s >= d.NZ) kz = s - d.NZ + d.NZH;
       if (kz >= 0) {
         float2 o = make_float2(__fmul_rn(y[q].x, sc), __fmul_rn(y[q].y, sc));
-        if (a.mean_split) {
-          const float2 l = mean_term(a, mr, j, kz, i);
+        if (lm) {
+          const float2 l = lm[(size_t)kz * d.NXH];
           o.x = __fadd_rn(o.x, l.x);
           o.y = __fadd_rn(o.y, l.y);
         }
