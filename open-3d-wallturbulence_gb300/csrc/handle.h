@@ -105,6 +105,10 @@ struct owt_handle {
   // device constants
   double *kx = nullptr, *kz = nullptr, *c11 = nullptr, *c21 = nullptr, *c22 = nullptr, *inv_cg = nullptr;
   double *nc21 = nullptr, *nc22 = nullptr;  // nu c21, nu c22
+  // the mode kernel's coefficients with the unscaling of its solved h d1,
+  // h^2 d2: c11/h, c21/h, c22/h^2, nu c21/h, nu c22/h^2
+  double *c11h = nullptr, *c21h = nullptr, *c22h = nullptr, *nc21h = nullptr, *nc22h = nullptr;
+  double *rs_gi = nullptr;  // omega_y-system row scales times 1/cg of the mode [n_g][U]
   // state
   double2 *v_ring = nullptr, *g_ring = nullptr, *hv_ring = nullptr, *hg_ring = nullptr, *q_ring = nullptr;
   double2 *u = nullptr, *w = nullptr, *ox = nullptr, *oz = nullptr, *lx = nullptr, *ly = nullptr, *lz = nullptr;

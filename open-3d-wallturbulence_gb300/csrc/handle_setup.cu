@@ -126,6 +126,20 @@ void owt_handle::setup(const owt_params &prm) {
     for (int j = 0; j < NY; ++j) { a21[j] = p.nu * grid.c21[j]; a22[j] = p.nu * grid.c22[j]; }
     nc21 = upload(a21, owned, st);
     nc22 = upload(a22, owned, st);
+    const double ih = 1.0 / grid.ds, ih2 = 1.0 / (grid.ds * grid.ds);
+    std::vector<double> h11(NY), h21(NY), h22(NY), hn21(NY), hn22(NY);
+    for (int j = 0; j < NY; ++j) {
+      h11[j] = grid.c11[j] * ih;
+      h21[j] = grid.c21[j] * ih;
+      h22[j] = grid.c22[j] * ih2;
+      hn21[j] = a21[j] * ih;
+      hn22[j] = a22[j] * ih2;
+    }
+    c11h = upload(h11, owned, st);
+    c21h = upload(h21, owned, st);
+    c22h = upload(h22, owned, st);
+    nc21h = upload(hn21, owned, st);
+    nc22h = upload(hn22, owned, st);
   }
   inv_cg = upload(icg, owned, st);
   d_step = dalloc<long long>(1, owned);
@@ -153,6 +167,9 @@ void owt_handle::setup(const owt_params &prm) {
   };
   factor(bv, tv, Uq, d_sa, d_sb, true);
   factor(bg, tg, Uq, d_icg, nullptr, true);
+  rs_gi = dalloc<double>((size_t)bg.n * Uq, owned);
+  launch_scale_by_mode(rs_gi, bg.rscale, inv_cg, bg.n, Uq, st);
+  ++launches;
   factor(b1, t1, 1, nullptr, nullptr, false);
   factor(b2, t2, 1, nullptr, nullptr, false);
   int herr = 0;

@@ -110,17 +110,16 @@ ModeArgs owt_handle::mode_args() const {
   a.NY = NY; a.NZ = NZ; a.NXH = NXH; a.NZH = NZH; a.M = M; a.U = Uq;
   a.u0 = 0; a.u1 = Uq;
   a.inv_dt = 1.0 / p.dt; a.nu = p.nu;
-  a.kx = kx; a.kz = kz; a.c11 = c11; a.c21 = c21; a.c22 = c22;
+  a.kx = kx; a.kz = kz;
   a.v_ring = v_ring; a.g_ring = g_ring; a.hv_ring = hv_ring; a.hg_ring = hg_ring; a.q_ring = q_ring;
   a.u_out = u; a.w_out = w; a.ox_out = ox; a.oz_out = oz;
   a.ab_v = bv.ab; a.piv_v = bv.piv; a.n_v = bv.n;
   a.ab_g = bg.ab; a.piv_g = bg.piv; a.n_g = bg.n;
   a.rhs_node_v = rhs_node_v; a.rb_col = rb_col; a.rb_val = rb_val; a.inv_cg = inv_cg;
-  a.rs_v = bv.rscale; a.rs_g = bg.rscale;
-  a.inv_h = 1.0 / grid.ds; a.inv_h2 = 1.0 / (grid.ds * grid.ds);
+  a.rs_v = bv.rscale; a.rs_gi = rs_gi;
   a.sg = sg; a.dg = dg; a.yv = yv; a.yg = yg; a.sv = sv;
   a.rbv_col = rbv_col; a.rbv_val = rbv_val;
-  a.nc21 = nc21; a.nc22 = nc22;
+  a.c11h = c11h; a.c21h = c21h; a.c22h = c22h; a.nc21h = nc21h; a.nc22h = nc22h;
   a.step = d_step;
   a.vw = vw_on ? vw : nullptr;
   return a;

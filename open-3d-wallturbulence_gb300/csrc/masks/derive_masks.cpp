@@ -16,7 +16,7 @@
 #include <vector>
 using namespace owt;
 struct Stat { unsigned long long L[8] = {0}, U[8] = {0}, P[8] = {0}; };
-static void factor_and_scan(const BandTemplate &t, double s1, double s2, int NT, int OFF, int EDGE, Stat &st) {
+static void factor_and_scan(const BandTemplate &t, double s1, double s2, int NT, int OFF, int LO, int HI, Stat &st) {
   const int n = t.n, KL = t.kl, KU = t.ku, KV = KL + KU, NB = 2 * KL + KU + 1;
   std::vector<double> ab((size_t)NB * n, 0.0);
   auto AB = [&](int b, int c) -> double & { return ab[(size_t)b * n + c]; };
@@ -40,7 +40,7 @@ static void factor_and_scan(const BandTemplate &t, double s1, double s2, int NT,
     for (int i = 1; i <= km; ++i) AB(KV + i, j) *= rp;
     for (int c = j + 1; c <= ju; ++c) { const double tt = AB(KV - (c - j), c); if (tt != 0.0) for (int i = 1; i <= km; ++i) AB(KV + i - (c - j), c) -= AB(KV + i, j) * tt; }
   }
-  for (int c = EDGE; c < n - EDGE; ++c) {
+  for (int c = LO; c < n - HI; ++c) {
     const int ty = (c + OFF) % NT;
     for (int tt = 1; tt <= KL; ++tt) if (AB(KV + tt, c) != 0.0) st.L[ty] |= 1ull << tt;
     for (int tt = 1; tt <= KV; ++tt) if (AB(KV - tt, c) != 0.0) st.U[ty] |= 1ull << tt;
@@ -66,8 +66,10 @@ int main() {
       for (int q = 0; q <= 40; ++q) {
         const double k = q == 0 ? 0.0 : 0.2 * std::pow(1500.0 / 0.2, (q - 1) / 39.0);
         const double k2 = k * k;
-        factor_and_scan(tv, g0 / cf.dt + 2 * cf.nu * k2, cf.nu * k2 * k2 + g0 * k2 / cf.dt, 4, 2, 48, sv);
-        factor_and_scan(tg, 1.0 / (cf.nu * k2 + g0 / cf.dt), 0.0, 2, 0, 60, sg);
+        // the full-band widths at both ends (VMasks, VMasks6, GMasks)
+        factor_and_scan(tv, g0 / cf.dt + 2 * cf.nu * k2, cf.nu * k2 * k2 + g0 * k2 / cf.dt, 4, 2, order == 8 ? 40 : 44,
+                        order == 8 ? 32 : 24, sv);
+        factor_and_scan(tg, 1.0 / (cf.nu * k2 + g0 / cf.dt), 0.0, 2, 0, 16, 16, sg);
       }
     }
     std::printf("order %d\n v L:", order); for (int i = 0; i < 4; ++i) std::printf(" 0x%llx", sv.L[i]);

@@ -71,30 +71,42 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
   double *yv = reinterpret_cast<double *>(a.yv) + comp;
   double *yg = reinterpret_cast<double *>(a.yg) + comp;
   auto E = [&](int j) { return 2 * ((size_t)j * M + m); };  // offset of (j, m) in doubles
-  const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0, be1 = -3.0, be2 = 1.0;
+  // (be1 = -be0 and be2 = 1 are used in the form of step 1)
+  const double al0 = 3.0, al1 = -1.5, al2 = 1.0 / 3.0, be0 = 3.0;
   const double idt = a.inv_dt;
 
   // 1. source_g, walls zero (solver.cpp:573-574, 598-599), and source_v on
-  //    the nodes with an interior equation (solver.cpp:569-571, 590-596)
+  //    the nodes with an interior equation (solver.cpp:569-571, 590-596).
+  //    The beta sum 3 H0 - 3 H1 + H2 is formed as 3 (H0 - H1) + H2, and 1/dt
+  //    (and -k^2/dt for v) is folded into the alpha weights: two and three
+  //    FP64 operations fewer per node than the sums as written.
   {
     const double k2dt = k2 * idt;
+    const double ag0 = al0 * idt, ag1 = al1 * idt, ag2 = al2 * idt;
+    const double av0 = -k2dt * al0, av1 = -k2dt * al1, av2 = -k2dt * al2;
     for (int j = 0; j < NY; ++j) {
       const size_t e = E(j);
       double r = 0.0;
       if (j != 0 && j != NY - 1)
-        r = (hg0[e] * be0 + hg1[e] * be1 + hg2[e] * be2) + (g0[e] * al0 + g1[e] * al1 + g2[e] * al2) * idt;
+        r = fma(g2[e], ag2, fma(g1[e], ag1, fma(g0[e], ag0, fma(hg0[e] - hg1[e], be0, hg2[e]))));
       sg[e] = r;
       double rv = 0.0;
       if (j >= 2 && j <= NY - 3) {
-        const double vs = v0[e] * al0 + v1[e] * al1 + v2[e] * al2;
-        const double qs = q0[e] * al0 + q1[e] * al1 + q2[e] * al2;
-        rv = (hv0[e] * be0 + hv1[e] * be1 + hv2[e] * be2) - k2dt * vs + qs * idt;
+        rv = fma(hv0[e] - hv1[e], be0, hv2[e]);
+        rv = fma(v0[e], av0, rv);
+        rv = fma(v1[e], av1, rv);
+        rv = fma(v2[e], av2, rv);
+        rv = fma(q0[e], ag0, rv);
+        rv = fma(q1[e], ag1, rv);
+        rv = fma(q2[e], ag2, rv);
       }
       sv[e] = rv;
     }
   }
 
-  // 2. omega_y-system: g and DY1 g
+  // 2. omega_y-system: g and DY1 g.  The solve gives h DY1 g and h^2 DY2 g;
+  //    the tables c11h, nc21h, nc22h carry the 1/h, 1/h^2 of the metric
+  //    coefficients, and rs_gi the 1/cg of the row scales.
   const double icg = a.inv_cg[u];
   {
     double d2 = 0.0;
@@ -102,21 +114,20 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
       double acc = 0.0;
 #pragma unroll
       for (int q = 0; q < 5; ++q) acc += a.rb_val[p * 5 + q] * sg[E(a.rb_col[p * 5 + q])];
-      return acc * (icg * a.rs_g[(size_t)p * a.U + u]);
+      return acc * a.rs_gi[(size_t)p * a.U + u];
     };
     auto ys = [&](int p, double y) { yg[E(p)] = y; };
     auto yl = [&](int p) -> double { return yg[E(p)]; };
     auto out = [&](int c, double x) {
       const int jn = c >> 1;
       if (c & 1) {
-        d2 = x * a.inv_h2;
+        d2 = x;
       } else {
-        x *= a.inv_h;
         const size_t e = E(jn);
         double g = 0.0;
-        if (jn != 0 && jn != NY - 1) g = (sg[e] + a.nc21[jn] * x + a.nc22[jn] * d2) * icg;
+        if (jn != 0 && jn != NY - 1) g = fma(a.nc22h[jn], d2, fma(a.nc21h[jn], x, sg[e])) * icg;
         gn[e] = g;
-        dg[e] = a.c11[jn] * x;
+        dg[e] = a.c11h[jn] * x;
       }
     };
     if (SPARSE) band_solve_g_sparse(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
@@ -129,9 +140,8 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
     const bool horiz = !(k2 < 1.e-8);
     const double ik2 = horiz ? 1.0 / k2 : 0.0;
     const double sgn = comp ? 1.0 : -1.0;
-    const double sax = sgn * kx * ik2, saz = sgn * kz * ik2, sik2 = sgn * ik2;
-    const double kzk2 = kz * k2, kxk2 = kx * k2;
-    double d1 = 0.0, d2 = 0.0;
+    const double sax = sgn * kx * ik2, saz = sgn * kz * ik2, skx = sgn * kx, skz = sgn * kz;
+    double d1 = 0.0, d2 = 0.0;  // h DY1 v, h^2 DY2 v of the node being finished
     auto rhs = [&](int p) -> double {
       const int tag = a.rhs_node_v[p];
       if (tag == kRhsTable) {
@@ -151,30 +161,30 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
       int t, jn;
       vcol_split(c, NY, t, jn);
       if (t == 2) {
-        d2 = x * a.inv_h2;
+        d2 = x;
       } else if (t == 1) {
-        d1 = x * a.inv_h;
+        d1 = x;
       } else if (t == 0) {
         const size_t e = E(jn);
         vn[e] = x;
-        const double q = a.c21[jn] * d1 + a.c22[jn] * d2;
+        const double q = fma(a.c22h[jn], d2, a.c21h[jn] * d1);
         qn[e] = q;
         if (horiz) {
-          const double dv = a.c11[jn] * d1;
+          const double dv = a.c11h[jn] * d1;
           const unsigned mask = __activemask();
           // the partner lane's component of v, DY1 v, DY2 v; of g, DY1 g from memory
           const double xo = __shfl_xor_sync(mask, x, 1), dvo = __shfl_xor_sync(mask, dv, 1),
                        qo = __shfl_xor_sync(mask, q, 1);
           const double go = gn[e + 1 - 2 * comp], dgo = dg[e + 1 - 2 * comp];
           // u = i kx/k2 DY1v - i kz/k2 g ; w = i kx/k2 g + i kz/k2 DY1v
-          // omega_x = i/k2 (kx DY1g + kz DY2v - kz k2 v) ; omega_z = i/k2 (kz DY1g - kx DY2v + kx k2 v)
+          // omega_x = i/k2 (kx DY1g + kz DY2v) - i kz v ; omega_z = i/k2 (kz DY1g - kx DY2v) + i kx v
           // component c of i z is (2c - 1) times the other component of z
           double *uo = reinterpret_cast<double *>(a.u_out), *wo = reinterpret_cast<double *>(a.w_out);
           double *oxo = reinterpret_cast<double *>(a.ox_out), *ozo = reinterpret_cast<double *>(a.oz_out);
           uo[e + comp] = sax * dvo - saz * go;
           wo[e + comp] = sax * go + saz * dvo;
-          oxo[e + comp] = (kx * dgo + kz * qo - kzk2 * xo) * sik2;
-          ozo[e + comp] = (kz * dgo - kx * qo + kxk2 * xo) * sik2;
+          oxo[e + comp] = fma(-skz, xo, fma(saz, qo, sax * dgo));
+          ozo[e + comp] = fma(skx, xo, fma(-sax, qo, saz * dgo));
         }
       }
     };

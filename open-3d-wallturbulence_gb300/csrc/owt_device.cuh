@@ -358,14 +358,16 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // stretchings, found by factorising the band templates on the host over such
 // a sweep; every factorization is checked against them
 // (k_check_pattern) and the full-band solve is used if any mode falls
-// outside.  Columns within EDGE of either end are always swept with the full
-// band.  Register rings are padded to multiples of NT so that the unknown type
+// outside.  The first Masks::lo and the last Masks::hi columns keep the
+// boundary closures' own fill and are swept with the full band: the widths
+// are those beyond which the sweep found every column inside its type's masks
+// (eighth order: columns up to 38 from the bottom and 29 from the top lie
+// outside, sixth order 42 and 21, the omega_y-system 11 and 9), rounded up.
+// Register rings are padded to multiples of NT so that the unknown type
 // of every unrolled step is a compile-time constant (n is a multiple of NT).
 // Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward),
 // row interchange with offset t may occur (pivots).
 // ---------------------------------------------------------------------------
-constexpr int VB_EDGE = 48;
-constexpr int GB_EDGE = 60;
 // v-system (v, d1, d2, d3 per interior node): 26.25 entries per column
 // instead of 43 (the reference's eighth-order operators; the sixth-order
 // option has masks of its own, vmask6_* / VMasks6 below, checked at setup by
@@ -385,6 +387,7 @@ __host__ __device__ constexpr unsigned long long vmask_p(int ty) {
 __host__ __device__ constexpr unsigned long long gmask_l(int ty) { return ty == 0 ? 0x3eull : 0x1eull; }
 __host__ __device__ constexpr unsigned long long gmask_u(int ty) { return ty == 0 ? 0x1eull : 0x3eull; }
 struct VMasks {
+  static constexpr int lo = 40, hi = 32;
   __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask_p(ty); }
@@ -401,17 +404,19 @@ __host__ __device__ constexpr unsigned long long vmask6_p(int ty) {
   return ty == 0 ? 0x5eull : ty == 1 ? 0x1eull : ty == 2 ? 0x12ull : 0x8cull;
 }
 struct VMasks6 {
+  static constexpr int lo = 44, hi = 24;
   __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask6_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask6_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask6_p(ty); }
 };
 struct GMasks {
+  static constexpr int lo = 16, hi = 16;
   __host__ __device__ static constexpr unsigned long long l(int ty) { return gmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return gmask_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int) { return 0ull; }
 };
 
-template <int KL, int KU, int NT, int OFF, int W, int WB, int EDGE, class Masks, class Rhs, class YStore,
+template <int KL, int KU, int NT, int OFF, int W, int WB, class Masks, class Rhs, class YStore,
           class YLoad, class Out>
 __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                   int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
@@ -425,7 +430,7 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
 #pragma unroll
     for (int t = 0; t < W; ++t) w[t] = (t < n) ? rhs(t) : vzero<V>();
     for (int j0 = 0; j0 < n; j0 += W) {
-      const bool sparse = (j0 >= EDGE) && (j0 + W - 1 < n - EDGE);
+      const bool sparse = (j0 >= Masks::lo) && (j0 + W - 1 < n - Masks::hi);
 #pragma unroll
       for (int s = 0; s < W; ++s) {
         const int j = j0 + s;
@@ -463,7 +468,7 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
     for (int jj = 0; jj < n; jj += WB) {
       // columns n-1-jj .. n-1-jj-(WB-1); the type of column n-1-jj-s is
       // (OFF - 1 - s) mod NT
-      const bool sparse = (n - 1 - jj < n - EDGE) && (n - 1 - jj - (WB - 1) >= EDGE);
+      const bool sparse = (n - 1 - jj < n - Masks::hi) && (n - 1 - jj - (WB - 1) >= Masks::lo);
 #pragma unroll
       for (int s = 0; s < WB; ++s) {
         const int j = n - 1 - (jj + s);
@@ -492,13 +497,13 @@ template <class VM = VMasks, class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<15, 13, 4, 2, 16, 32, VB_EDGE, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<15, 13, 4, 2, 16, 32, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<6, 6, 2, 0, 8, 14, GB_EDGE, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<6, 6, 2, 0, 8, 14, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 
 // ---------------------------------------------------------------------------

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstring>
 #include <random>
 #include <vector>
@@ -331,8 +332,8 @@ void launch_modes_batch(const BatchTable<ModeArgs> &t, int variant, int *work, i
 
 // Every factored system must keep its interior fill inside the masks of its
 // masked solve: count the modes whose L or U has a nonzero outside the masks
-// in columns [EDGE, n - EDGE).
-template <int KL, int KU, int NT, int OFF, int EDGE, class Masks>
+// in columns [Masks::lo, n - Masks::hi).
+template <int KL, int KU, int NT, int OFF, class Masks>
 __global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n, int U,
                                 int *__restrict__ bad) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,7 +341,7 @@ __global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__
   constexpr int KV = KL + KU;
   const size_t sn = (size_t)n * U;
   int nbad = 0;
-  for (int c = EDGE; c < n - EDGE; ++c) {
+  for (int c = Masks::lo; c < n - Masks::hi; ++c) {
     const int ty = (c + OFF) % NT;
     const double *col = ab + (size_t)c * U + u;
     for (int t = 1; t <= KL; ++t)
@@ -359,13 +360,26 @@ __global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
                           cudaStream_t st) {
   if (which == 0)
-    k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+    k_check_pattern<15, 13, 4, 2, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
   else if (which == 2)
-    k_check_pattern<15, 13, 4, 2, VB_EDGE, VMasks6><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+    k_check_pattern<15, 13, 4, 2, VMasks6><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
   else
-    k_check_pattern<6, 6, 2, 0, GB_EDGE, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+    k_check_pattern<6, 6, 2, 0, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
 }
 void launch_modes_sixth(const ModeArgs &a, cudaStream_t st) { modes_sixth_launch(a, st); }
+
+// dst[p U + u] = scale[u] src[p U + u] (setup: per-mode factors folded into
+// a [row][unique mode] table)
+__global__ void k_scale_by_mode(double *dst, const double *src, const double *scale, int n, int U) {
+  const size_t total = (size_t)n * U;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    dst[e] = scale[e % U] * src[e];
+}
+void launch_scale_by_mode(double *dst, const double *src, const double *scale, int n, int U, cudaStream_t st) {
+  const size_t total = (size_t)n * U;
+  const unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, 4096);
+  k_scale_by_mode<<<blocks, 256, 0, st>>>(dst, src, scale, n, U);
+}
 
 __global__ void k_advance(long long *step) { *step += 1; }
 void launch_advance(long long *step, cudaStream_t st) { k_advance<<<1, 1, 0, st>>>(step); }

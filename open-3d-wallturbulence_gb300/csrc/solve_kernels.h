@@ -33,7 +33,7 @@ struct ModeArgs {
   int NY, NZ, NXH, NZH, M, U;
   int u0, u1;  // quad mapping: unique modes u0 <= u < u1 only (0, U: all)
   double inv_dt, nu;
-  const double *kx, *kz, *c11, *c21, *c22;
+  const double *kx, *kz;
   double2 *v_ring, *g_ring, *hv_ring, *hg_ring, *q_ring;  // 3 slots each, [slot][y][mode]
   double2 *u_out, *w_out, *ox_out, *oz_out;
   const double *ab_v; const uint8_t *piv_v; int n_v;
@@ -41,13 +41,15 @@ struct ModeArgs {
   const int *rhs_node_v;
   const int *rb_col; const double *rb_val;
   const double *inv_cg;
-  const double *rs_v, *rs_g;  // inverse row scales [n][U]
-  double inv_h, inv_h2;       // unscaling of solved h d1, h^2 d2
+  const double *rs_v;   // inverse row scales [n][U]
+  const double *rs_gi;  // inverse row scales of the omega_y-system times 1/cg of the mode [n][U]
   double2 *sg, *dg, *yv, *yg, *sv;  // scratch
   const long long *step;
   const double2 *vw;  // wall-normal velocity at the walls [2][M] (bottom, top), or null
   const int *rbv_col; const double *rbv_val;  // v-system rhs tables [n_v][4]
-  const double *nc21, *nc22;                  // nu c21, nu c22
+  // metric coefficients with the unscaling of the solved h d1, h^2 d2:
+  // c11/h, c21/h, c22/h^2, nu c21/h, nu c22/h^2 [NY]
+  const double *c11h, *c21h, *c22h, *nc21h, *nc22h;
 };
 
 struct MeanArgs {
@@ -148,6 +150,8 @@ void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, 
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st);
 int modes_pair_count();  // variants below this index use the pair mapping, the others the quad mapping
 void launch_modes_sixth(const ModeArgs &a, cudaStream_t st);  // masked solve with the sixth-order fill
+// dst[p U + u] = scale[u] src[p U + u], p < n
+void launch_scale_by_mode(double *dst, const double *src, const double *scale, int n, int U, cudaStream_t st);
 int modes_variant_count();
 const char *modes_variant_name(int v);
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
