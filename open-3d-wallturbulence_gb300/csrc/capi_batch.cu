@@ -237,7 +237,7 @@ struct owt_batch {
       ck(cudaEventCreate(&e0), "event");
       ck(cudaEventCreate(&e1), "event");
       float best = 1e30f;
-      for (int v = 0; v < modes_variant_count(); ++v) {
+      for (int v = 0; v < modes_batch_variant_count(); ++v) {
         build_modes(v, true);
         launch_modes_all(st);  // warm-up
         ck(cudaEventRecord(e0, st), "event");

@@ -489,7 +489,7 @@ void owt_handle::step_host(const double *const *hist, const double *means, const
   ensure_tuned();
   ck(cudaStreamSynchronize(st), "host step");
   const int variant = forced_variant >= 0 ? forced_variant : modes_variant;
-  const bool quad = modes_sparse() && !sparse_v6 && variant >= modes_pair_count();
+  const bool quad = modes_sparse() && !sparse_v6 && modes_variant_is_quad(variant);
   const int want = host_chunks > 0 ? host_chunks : HostStep::kDefaultChunks;
   const int nchunk = quad ? std::min(std::min(want, HostStep::kChunks), NZH + 1) : 1;
   // means first (the mean-mode kernel starts with the step)

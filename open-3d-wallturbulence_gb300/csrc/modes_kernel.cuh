@@ -21,14 +21,31 @@ namespace owt {
 //     combinations of source_v (the fourth-derivative rows into which the
 //     interior equations were substituted)
 //  5. solve_horizontal's velocity/vorticity from v, g    (solver.cpp:532-536)
+//
+// ROLE 0: one thread does all of it.  ROLE 1 and 2 (the split mapping, pair
+// lanes only): a warp of ROLE 1 does steps 1 and 2 for 16 modes and a warp
+// of ROLE 2 steps 1, 3-5 for the same modes; the v-system's forward sweep
+// runs beside the omega_y solve, and named barrier `bar` (the two warps, 64
+// threads; every thread of both arrives exactly once, active or not) orders
+// the omega_y results before the backward sweep that reads them.  Each value
+// is computed by the same operations as in ROLE 0.
 // ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, class VM = VMasks>
-__device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, class VM = VMasks, int ROLE = 0>
+__device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid, const int bar = 0) {
+  static_assert(ROLE == 0 || (!QUAD && SPARSE), "the split mapping pairs lanes and runs the masked solves");
   // One thread per real component of a mode (the band systems are real).
   // Pair mapping: lanes 2m, 2m+1 are Re, Im of mode m.  Quad mapping: lanes
   // 4u..4u+3 are (Re, Im) of the two modes +kz, -kz of unique mode u, which
   // share one factorization, so four adjacent lanes read the same factors.
   int m, comp, k, i, kabs;
+  const bool active = QUAD || (tid >> 1) < a.M;
   if (QUAD) {
     const int uq = a.u0 + (tid >> 2), r = tid & 3, sgn = r >> 1;
     comp = r & 1;
@@ -41,7 +58,10 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
   } else {
     m = tid >> 1;
     comp = tid & 1;
-    if (m >= a.M) return;
+    if (m >= a.M) {
+      if (ROLE == 0) return;
+      m = 0;  // an idle lane of the split mapping: no work, but it arrives at the barrier
+    }
     k = m / a.NXH;
     i = m - k * a.NXH;
     kabs = (k <= a.NZH) ? k : a.NZ - k;
@@ -84,31 +104,35 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
     const double k2dt = k2 * idt;
     const double ag0 = al0 * idt, ag1 = al1 * idt, ag2 = al2 * idt;
     const double av0 = -k2dt * al0, av1 = -k2dt * al1, av2 = -k2dt * al2;
-    for (int j = 0; j < NY; ++j) {
+    for (int j = 0; j < NY && active; ++j) {
       const size_t e = E(j);
-      double r = 0.0;
-      if (j != 0 && j != NY - 1)
-        r = fma(g2[e], ag2, fma(g1[e], ag1, fma(g0[e], ag0, fma(hg0[e] - hg1[e], be0, hg2[e]))));
-      sg[e] = r;
-      double rv = 0.0;
-      if (j >= 2 && j <= NY - 3) {
-        rv = fma(hv0[e] - hv1[e], be0, hv2[e]);
-        rv = fma(v0[e], av0, rv);
-        rv = fma(v1[e], av1, rv);
-        rv = fma(v2[e], av2, rv);
-        rv = fma(q0[e], ag0, rv);
-        rv = fma(q1[e], ag1, rv);
-        rv = fma(q2[e], ag2, rv);
+      if (ROLE != 2) {
+        double r = 0.0;
+        if (j != 0 && j != NY - 1)
+          r = fma(g2[e], ag2, fma(g1[e], ag1, fma(g0[e], ag0, fma(hg0[e] - hg1[e], be0, hg2[e]))));
+        sg[e] = r;
       }
-      sv[e] = rv;
+      if (ROLE != 1) {
+        double rv = 0.0;
+        if (j >= 2 && j <= NY - 3) {
+          rv = fma(hv0[e] - hv1[e], be0, hv2[e]);
+          rv = fma(v0[e], av0, rv);
+          rv = fma(v1[e], av1, rv);
+          rv = fma(v2[e], av2, rv);
+          rv = fma(q0[e], ag0, rv);
+          rv = fma(q1[e], ag1, rv);
+          rv = fma(q2[e], ag2, rv);
+        }
+        sv[e] = rv;
+      }
     }
   }
 
   // 2. omega_y-system: g and DY1 g.  The solve gives h DY1 g and h^2 DY2 g;
   //    the tables c11h, nc21h, nc22h carry the 1/h, 1/h^2 of the metric
   //    coefficients, and rs_gi the 1/cg of the row scales.
-  const double icg = a.inv_cg[u];
-  {
+  if (ROLE != 2 && active) {
+    const double icg = a.inv_cg[u];
     double d2 = 0.0;
     auto rhs = [&](int p) -> double {
       double acc = 0.0;
@@ -133,7 +157,12 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
     if (SPARSE) band_solve_g_sparse(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
     else band_solve<KLG, KUG>(a.ab_g, a.piv_g, a.n_g, a.U, u, rhs, ys, yl, out);
   }
-  __syncwarp(__activemask());  // the partner's g, DY1 g are read below
+  if (ROLE == 0) __syncwarp(__activemask());  // the partner's g, DY1 g are read below
+  if (ROLE == 1) {
+    __threadfence_block();  // g, DY1 g before the v warp's backward sweep reads them
+    named_bar_arrive(bar, 64);
+    return;
+  }
 
   // 3-5. v-system, then solve_horizontal's components
   {
@@ -188,8 +217,13 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
         }
       }
     };
-    if (SPARSE) band_solve_v_sparse<VM>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
-    else band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    if (SPARSE) {
+      if (active) band_forward_v_sparse<VM>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys);
+      if (ROLE == 2) named_bar_sync(bar, 64);
+      if (active) band_backward_v_sparse<VM>(a.ab_v, a.n_v, a.U, u, yl, out);
+    } else {
+      band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    }
   }
 }
 
@@ -197,6 +231,17 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid) {
 template <int KLV, int KUV, int KLG, int KUG, bool SPARSE, bool QUAD, int BLOCK, int MINB, class VM = VMasks>
 __global__ void __launch_bounds__(BLOCK, MINB) k_modes(const __grid_constant__ ModeArgs a) {
   mode_body<KLV, KUV, KLG, KUG, SPARSE, QUAD, VM>(a, blockIdx.x * BLOCK + threadIdx.x);
+}
+
+// The split mapping: warp pairs (omega_y warp, v warp) over the pair
+// mapping's lanes; BLOCK/64 pairs per block, barrier ids 1 .. BLOCK/64.
+template <int KLV, int KUV, int KLG, int KUG, int BLOCK, int MINB, class VM = VMasks>
+__global__ void __launch_bounds__(BLOCK, MINB) k_modes_split(const __grid_constant__ ModeArgs a) {
+  static_assert(BLOCK % 64 == 0 && BLOCK / 64 <= 15, "warp pairs and named barriers");
+  const int w = threadIdx.x >> 5, pair = w >> 1;
+  const int tid = blockIdx.x * (BLOCK / 2) + pair * 32 + (threadIdx.x & 31);
+  if (w & 1) mode_body<KLV, KUV, KLG, KUG, true, false, VM, 2>(a, tid, 1 + pair);
+  else mode_body<KLV, KUV, KLG, KUG, true, false, VM, 1>(a, tid, 1 + pair);
 }
 
 // Every channel of a batch in one persistent launch.  Work items are the
@@ -234,6 +279,9 @@ const char *modes_pair_name(int v);
 void modes_pair_launch(int v, const ModeArgs &a, cudaStream_t st);
 void modes_dense_launch(const ModeArgs &a, cudaStream_t st);
 void modes_sixth_launch(const ModeArgs &a, cudaStream_t st);  // the sixth-order masks
+int modes_split_count();
+const char *modes_split_name(int v);
+void modes_split_launch(int v, const ModeArgs &a, cudaStream_t st);
 int modes_quad_count();
 const char *modes_quad_name(int v);
 void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st);

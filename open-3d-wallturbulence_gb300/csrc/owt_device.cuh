@@ -416,12 +416,13 @@ struct GMasks {
   __host__ __device__ static constexpr unsigned long long p(int) { return 0ull; }
 };
 
-template <int KL, int KU, int NT, int OFF, int W, int WB, class Masks, class Rhs, class YStore,
-          class YLoad, class Out>
-__device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
-                                                  int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
-                                                  Out out) {
-  static_assert(W >= KL + 1 && W % NT == 0 && WB >= KL + KU + 1 && WB % NT == 0, "ring sizes");
+// The forward sweep (row interchanges and L) and the backward sweep (U) of
+// band_solve_masked, which exchange the forward-swept values only through
+// ystore / yload; a caller may run other work between them.
+template <int KL, int KU, int NT, int OFF, int W, class Masks, class Rhs, class YStore>
+__device__ __forceinline__ void band_forward_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                    int n, int U, int u, Rhs rhs, YStore ystore) {
+  static_assert(W >= KL + 1 && W % NT == 0, "ring size");
   using V = decltype(rhs(0));
   constexpr int KV = KL + KU;
   const size_t sn = (size_t)n * U;
@@ -461,6 +462,13 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
       }
     }
   }
+}
+template <int KL, int KU, int NT, int OFF, int WB, class Masks, class V, class YLoad, class Out>
+__device__ __forceinline__ void band_backward_masked(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
+                                                     Out out) {
+  static_assert(WB >= KL + KU + 1 && WB % NT == 0, "ring size");
+  constexpr int KV = KL + KU;
+  const size_t sn = (size_t)n * U;
   {
     V w[WB];
 #pragma unroll
@@ -492,12 +500,32 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
   }
 }
 
+template <int KL, int KU, int NT, int OFF, int W, int WB, class Masks, class Rhs, class YStore,
+          class YLoad, class Out>
+__device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                  int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                  Out out) {
+  using V = decltype(rhs(0));
+  band_forward_masked<KL, KU, NT, OFF, W, Masks>(ab, piv, n, U, u, rhs, ystore);
+  band_backward_masked<KL, KU, NT, OFF, WB, Masks, V>(ab, n, U, u, yload, out);
+}
+
 // VM: VMasks (the reference's eighth-order operators) or VMasks6
 template <class VM = VMasks, class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
   band_solve_masked<15, 13, 4, 2, 16, 32, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
+}
+template <class VM = VMasks, class Rhs, class YStore>
+__device__ __forceinline__ void band_forward_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                      int n, int U, int u, Rhs rhs, YStore ystore) {
+  band_forward_masked<15, 13, 4, 2, 16, VM>(ab, piv, n, U, u, rhs, ystore);
+}
+template <class VM = VMasks, class YLoad, class Out>
+__device__ __forceinline__ void band_backward_v_sparse(const double *__restrict__ ab, int n, int U, int u,
+                                                       YLoad yload, Out out) {
+  band_backward_masked<15, 13, 4, 2, 32, VM, double>(ab, n, U, u, yload, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,

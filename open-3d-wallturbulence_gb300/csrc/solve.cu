@@ -307,15 +307,25 @@ bool band_supported(int kl, int ku) {
 
 // Mode-kernel variants live in modes_pair.cu and modes_quad.cu (separate
 // translation units so they compile in parallel); this dispatches by index.
-int modes_variant_count() { return modes_pair_count() + modes_quad_count(); }
+// Variants: the pair mapping's, then the quad mapping's, then the split
+// mapping's (single-channel launches only; batches choose among the first
+// two families).
+int modes_variant_count() { return modes_pair_count() + modes_quad_count() + modes_split_count(); }
+int modes_batch_variant_count() { return modes_pair_count() + modes_quad_count(); }
+bool modes_variant_is_quad(int v) { return v >= modes_pair_count() && v < modes_pair_count() + modes_quad_count(); }
 const char *modes_variant_name(int v) {
-  return v < modes_pair_count() ? modes_pair_name(v) : modes_quad_name(v - modes_pair_count());
+  if (v < modes_pair_count()) return modes_pair_name(v);
+  v -= modes_pair_count();
+  if (v < modes_quad_count()) return modes_quad_name(v);
+  return modes_split_name(v - modes_quad_count());
 }
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st) {
   if (!(klv == 15 && kuv == 13 && klg == 6 && kug == 6)) return;
   if (!sparse) { modes_dense_launch(a, st); return; }
-  if (variant < modes_pair_count()) modes_pair_launch(variant, a, st);
-  else modes_quad_launch(variant - modes_pair_count(), a, st);
+  if (variant < modes_pair_count()) { modes_pair_launch(variant, a, st); return; }
+  variant -= modes_pair_count();
+  if (variant < modes_quad_count()) modes_quad_launch(variant, a, st);
+  else modes_split_launch(variant - modes_quad_count(), a, st);
 }
 
 // Batched mode kernel: variant -1 is the full-band solve.

@@ -152,7 +152,9 @@ int modes_pair_count();  // variants below this index use the pair mapping, the 
 void launch_modes_sixth(const ModeArgs &a, cudaStream_t st);  // masked solve with the sixth-order fill
 // dst[p U + u] = scale[u] src[p U + u], p < n
 void launch_scale_by_mode(double *dst, const double *src, const double *scale, int n, int U, cudaStream_t st);
-int modes_variant_count();
+int modes_variant_count();        // single-channel launches: pair, quad, split mappings
+int modes_batch_variant_count();  // batched launches: pair and quad mappings
+bool modes_variant_is_quad(int v);
 const char *modes_variant_name(int v);
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
                           cudaStream_t st);

@@ -2,28 +2,31 @@
 
 The reference writes ``./DATA/F-%08d.H5`` every ``save_interval`` steps with
 datasets ``velx_real, velx_imag, vely_*, velz_*`` of global shape
-[NZ][NXH][NY] (src/IO.cpp:118-156, 198-235).  No HDF5 library is available
-here, so the same datasets, names and shapes go into ``F-%08d.npz``.
+[NZ][NXH][NY], float64 (src/IO.cpp:118-156, 198-235).  The same file, names,
+shapes and type are written here by ``owt.h5lite`` (the HDF5 file format
+written directly: no HDF5 library is installed with this package).
 """
 import os
 
 import numpy as np
 
+from . import h5lite
+
 
 def save_instant_field(solver, id_step, directory="DATA"):
     os.makedirs(directory, exist_ok=True)
-    path = os.path.join(directory, "F-%08d.npz" % id_step)
+    path = os.path.join(directory, "F-%08d.H5" % id_step)
     data = {}
     for name in ("velx", "vely", "velz"):
         f = solver.get(name)
         data[name + "_real"] = np.ascontiguousarray(f.real)
         data[name + "_imag"] = np.ascontiguousarray(f.imag)
-    np.savez(path, **data)
+    h5lite.write(path, data)
     return path
 
 
 def load_instant_field(path):
-    d = np.load(path)
+    d = h5lite.read(path)
     return {n: d[n + "_real"] + 1j * d[n + "_imag"] for n in ("velx", "vely", "velz")}
 
 

@@ -64,7 +64,7 @@ def test_snapshot_round_trip(gpu_lib, run, tmp_path):
     p, s = run
     s.time_Integration(2)
     path = save_instant_field(s, 2, directory=str(tmp_path / "DATA"))
-    assert path.endswith("F-00000002.npz")
+    assert path.endswith("F-00000002.H5")
     d = load_instant_field(path)
     for n in ("velx", "vely", "velz"):
         np.testing.assert_array_equal(d[n], s.get(n))
