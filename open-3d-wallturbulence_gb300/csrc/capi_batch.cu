@@ -301,7 +301,11 @@ int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
     }
     ck(cudaSetDevice(handles[0]->p.device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking), "stream");
-    ck(cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking), "stream");
+    {
+      int lo = 0, hi = 0;  // the mean modes' branch at the highest priority, as in a single channel's step
+      ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+      ck(cudaStreamCreateWithPriority(&b->st2, cudaStreamNonBlocking, hi), "stream");
+    }
     ck(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_fork2, cudaEventDisableTiming), "event");
@@ -316,7 +320,7 @@ int owt_batch_create(owt_handle *const *handles, int count, owt_batch **out) {
     ck(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "begin capture");
     b->enqueue();
     ck(cudaStreamEndCapture(b->st, &b->graph), "end capture");
-    ck(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate");
+    ck(cudaGraphInstantiate(&b->exec, b->graph, cudaGraphInstantiateFlagUseNodePriority), "instantiate");
     ck(cudaStreamSynchronize(b->st), "batch setup");
   } catch (const std::exception &e) {
     g_create_error = e.what();

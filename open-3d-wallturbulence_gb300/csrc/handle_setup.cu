@@ -73,7 +73,14 @@ void owt_handle::setup(const owt_params &prm) {
     throw OwtError(OWT_ERR_INVALID, "3NX/2 and 3NZ/2 need at most 8 FFT stages");
   ck(cudaSetDevice(p.device), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
-  ck(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
+  {
+    // the mean mode's branch at the highest priority: its single block must
+    // not wait for a slot behind the mode kernel's blocks (it would then add
+    // its whole duration to the step)
+    int lo = 0, hi = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+    ck(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, hi), "cudaStreamCreate");
+  }
   ck(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
   ck(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
   ck(cudaEventCreateWithFlags(&ev_fork2, cudaEventDisableTiming), "cudaEventCreate");

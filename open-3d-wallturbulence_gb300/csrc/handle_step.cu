@@ -156,7 +156,8 @@ void owt_handle::run_steps(int64_t n) {
       launches = before;
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       ck(e, "end capture");
-      ck(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+      // node priorities as the streams had them at capture
+      ck(cudaGraphInstantiate(&gexec, graph, cudaGraphInstantiateFlagUseNodePriority), "graph instantiate");
     }
     for (int64_t s = 0; s < n; ++s) {
       ck(cudaGraphLaunch(gexec, st), "graph launch");

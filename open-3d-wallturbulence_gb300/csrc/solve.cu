@@ -464,42 +464,40 @@ __device__ __forceinline__ void mean_body(const MeanArgs &a) {
     }
   }
   __syncthreads();
-  if (t < 2) {
-    double2 *U = (t == 0) ? a.U_ring : a.W_ring;
-    double2 *sg = scr + (size_t)t * NY;
-    double2 *yy = scr + 2 * (size_t)NY + (size_t)t * n;
-    double2 *dd = a.dy1 + (size_t)t * NY;
+  // one lane per real component of each profile: lanes 0, 1 U (Re, Im),
+  // lanes 2, 3 W; the factors are real, so each component is its own solve
+  // with the operations the complex solve applies to it
+  if (t < 4) {
+    const int q = t >> 1, comp = t & 1;
+    double *U = reinterpret_cast<double *>(q == 0 ? a.U_ring : a.W_ring) + comp;
+    const double *sg = reinterpret_cast<const double *>(scr + (size_t)q * NY) + comp;
+    double *yy = reinterpret_cast<double *>(scr + 2 * (size_t)NY + (size_t)q * n) + comp;
+    double *dd = reinterpret_cast<double *>(a.dy1 + (size_t)q * NY) + comp;
     const double icg = a.inv_cg0;
-    double2 d2 = make_double2(0.0, 0.0);
-    double2 *Un = U + (size_t)h * NY;
-    auto rhs = [&](int p) -> double2 {
-      double2 acc = make_double2(0.0, 0.0);
-      for (int e = 0; e < 5; ++e) {
-        const double b = rbv[p * 5 + e];
-        const double2 r = sg[rbc[p * 5 + e]];
-        acc.x += b * r.x;
-        acc.y += b * r.y;
-      }
+    double d2 = 0.0;
+    double *Un = U + 2 * (size_t)h * NY;
+    auto rhs = [&](int p) -> double {
+      double acc = 0.0;
+      for (int e = 0; e < 5; ++e) acc += rbv[p * 5 + e] * sg[2 * rbc[p * 5 + e]];
       const double sc = icg * rs[(size_t)p * stride];
-      return make_double2(acc.x * sc, acc.y * sc);
+      return acc * sc;
     };
-    auto ys = [&](int p, double2 y) { yy[p] = y; };
-    auto yl = [&](int p) -> double2 { return yy[p]; };
-    auto out = [&](int c, double2 x) {
+    auto ys = [&](int p, double y) { yy[2 * p] = y; };
+    auto yl = [&](int p) -> double { return yy[2 * p]; };
+    auto out = [&](int c, double x) {
       const int jn = c >> 1;
       if (c & 1) {
-        d2 = make_double2(x.x * a.inv_h2, x.y * a.inv_h2);
+        d2 = x * a.inv_h2;
       } else {
-        x = make_double2(x.x * a.inv_h, x.y * a.inv_h);
-        double2 g = make_double2(0.0, 0.0);
+        x = x * a.inv_h;
+        double g = 0.0;
         if (jn != 0 && jn != NY - 1) {
-          const double2 r = sg[jn];
+          const double r = sg[2 * jn];
           const double w1 = a.nu * c21[jn], w2 = a.nu * c22[jn];
-          g.x = (r.x + w1 * x.x + w2 * d2.x) * icg;
-          g.y = (r.y + w1 * x.y + w2 * d2.y) * icg;
+          g = (r + w1 * x + w2 * d2) * icg;
         }
-        Un[jn] = g;
-        dd[jn] = make_double2(c11[jn] * x.x, c11[jn] * x.y);
+        Un[2 * jn] = g;
+        dd[2 * jn] = c11[jn] * x;
       }
     };
     band_solve<6, 6>(ab, piv, n, stride, 0, rhs, ys, yl, out);
