@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
 
 void launch_adj_modes(const AdjModeArgs &a, cudaStream_t st) {
   const int threads = 2 * a.M;
-  k_adj_modes<15, 13, 6, 6><<<(threads + 127) / 128, 128, 0, st>>>(a);
+  k_adj_modes<kVKL, kVKU, 6, 6><<<(threads + 127) / 128, 128, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------

@@ -95,7 +95,7 @@ void owt_handle::setup(const owt_params &prm) {
   BandTemplate t1 = build_plain_band(sten, 0);
   BandTemplate t2 = build_plain_band(sten, 1);
   // the kernels are specialised for the bands of the reference's stencils
-  pad_band(tv, 15, 13);
+  pad_band(tv, kVKL, kVKU);
   pad_band(tg, 6, 6);
   for (const BandTemplate *t : {&tv, &tg, &t1, &t2})
     if (!band_supported(t->kl, t->ku))

@@ -61,14 +61,13 @@ int main() {
     for (const Cfg &cf : cfgs) {
       Grid g = make_grid(cf.N, cf.alpha); Stencils st = make_stencils(cf.N, g.ds, order);
       BandTemplate tv = build_v_system(g, st, cf.nu), tg = build_g_system(g, st, cf.nu);
-      pad_band(tv, 15, 13); pad_band(tg, 6, 6);
+      pad_band(tv, kVKL, kVKU); pad_band(tg, 6, 6);
       const double g0 = 11.0 / 6.0;
       for (int q = 0; q <= 40; ++q) {
         const double k = q == 0 ? 0.0 : 0.2 * std::pow(1500.0 / 0.2, (q - 1) / 39.0);
         const double k2 = k * k;
         // the full-band widths at both ends (VMasks, VMasks6, GMasks)
-        factor_and_scan(tv, g0 / cf.dt + 2 * cf.nu * k2, cf.nu * k2 * k2 + g0 * k2 / cf.dt, 4, 2, order == 8 ? 40 : 44,
-                        order == 8 ? 32 : 24, sv);
+        factor_and_scan(tv, g0 / cf.dt + 2 * cf.nu * k2, cf.nu * k2 * k2 + g0 * k2 / cf.dt, 4, 2, 44, 32, sv);
         factor_and_scan(tg, 1.0 / (cf.nu * k2 + g0 / cf.dt), 0.0, 2, 0, 16, 16, sg);
       }
     }

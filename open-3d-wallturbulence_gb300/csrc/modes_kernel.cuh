@@ -170,7 +170,7 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid, cons
     const double ik2 = horiz ? 1.0 / k2 : 0.0;
     const double sgn = comp ? 1.0 : -1.0;
     const double sax = sgn * kx * ik2, saz = sgn * kz * ik2, skx = sgn * kx, skz = sgn * kz;
-    double d1 = 0.0, d2 = 0.0;  // h DY1 v, h^2 DY2 v of the node being finished
+    double xv = 0.0, d1 = 0.0, d2 = 0.0;  // v, h DY1 v, h^2 DY2 v of the node being finished
     auto rhs = [&](int p) -> double {
       const int tag = a.rhs_node_v[p];
       if (tag == kRhsTable) {
@@ -189,11 +189,22 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid, cons
     auto out = [&](int c, double x) {
       int t, jn;
       vcol_split(c, NY, t, jn);
+      // the backward sweep gives a node's unknowns in falling column order:
+      // at the four wall nodes d2, d1, then v; at interior nodes (reversed
+      // order) v, d1, then d2.  The node is finished with the last of the three.
+      const bool wall = jn < 2 || jn >= NY - 2;
+      bool last = false;
       if (t == 2) {
         d2 = x;
+        last = !wall;
       } else if (t == 1) {
         d1 = x;
       } else if (t == 0) {
+        xv = x;
+        last = wall;
+      }
+      if (last) {
+        x = xv;
         const size_t e = E(jn);
         vn[e] = x;
         const double q = fma(a.c22h[jn], d2, a.c21h[jn] * d1);

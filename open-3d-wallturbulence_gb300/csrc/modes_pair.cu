@@ -11,9 +11,9 @@ struct Variant {
   void (*batch)(BatchTable<ModeArgs>, int *);
 };
 const Variant kVariants[] = {
-    {"pair/128/r166", 128, k_modes<15, 13, 6, 6, true, false, 128, 3>, k_modes_batch<15, 13, 6, 6, true, false, 128, 3>},
-    {"pair/128/r128", 128, k_modes<15, 13, 6, 6, true, false, 128, 4>, k_modes_batch<15, 13, 6, 6, true, false, 128, 4>},
-    {"pair/256/r128", 256, k_modes<15, 13, 6, 6, true, false, 256, 2>, k_modes_batch<15, 13, 6, 6, true, false, 256, 2>},
+    {"pair/128/r166", 128, k_modes<kVKL, kVKU, 6, 6, true, false, 128, 3>, k_modes_batch<kVKL, kVKU, 6, 6, true, false, 128, 3>},
+    {"pair/128/r128", 128, k_modes<kVKL, kVKU, 6, 6, true, false, 128, 4>, k_modes_batch<kVKL, kVKU, 6, 6, true, false, 128, 4>},
+    {"pair/256/r128", 256, k_modes<kVKL, kVKU, 6, 6, true, false, 256, 2>, k_modes_batch<kVKL, kVKU, 6, 6, true, false, 256, 2>},
 };
 
 // resident blocks of a batched kernel on the current device
@@ -37,14 +37,14 @@ void modes_pair_launch(int v, const ModeArgs &a, cudaStream_t st) {
 // full-band solve (used when a factorization falls outside the sparse masks)
 void modes_dense_launch(const ModeArgs &a, cudaStream_t st) {
   const int bs = 128;
-  k_modes<15, 13, 6, 6, false, false, 128, 3><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
+  k_modes<kVKL, kVKU, 6, 6, false, false, 128, 3><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
 }
 
 // masked solve with the sixth-order fill (one variant: the sixth-order option
 // is not autotuned)
 void modes_sixth_launch(const ModeArgs &a, cudaStream_t st) {
   const int bs = 128;
-  k_modes<15, 13, 6, 6, true, false, 128, 3, VMasks6><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
+  k_modes<kVKL, kVKU, 6, 6, true, false, 128, 3, VMasks6><<<(unsigned)((2 * (long long)a.M + bs - 1) / bs), bs, 0, st>>>(a);
 }
 
 ModeBatchShape modes_pair_batch_shape(int v) {
@@ -57,10 +57,10 @@ void modes_pair_batch_launch(int v, const BatchTable<ModeArgs> &t, int *work, in
 }
 
 ModeBatchShape modes_dense_batch_shape() {
-  return {128, false, resident(k_modes_batch<15, 13, 6, 6, false, false, 128, 3>, 128)};
+  return {128, false, resident(k_modes_batch<kVKL, kVKU, 6, 6, false, false, 128, 3>, 128)};
 }
 void modes_dense_batch_launch(const BatchTable<ModeArgs> &t, int *work, int grid, cudaStream_t st) {
-  k_modes_batch<15, 13, 6, 6, false, false, 128, 3><<<grid, 128, 0, st>>>(t, work);
+  k_modes_batch<kVKL, kVKU, 6, 6, false, false, 128, 3><<<grid, 128, 0, st>>>(t, work);
 }
 
 }  // namespace owt

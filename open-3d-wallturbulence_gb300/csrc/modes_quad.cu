@@ -11,9 +11,9 @@ struct Variant {
   void (*batch)(BatchTable<ModeArgs>, int *);
 };
 const Variant kVariants[] = {
-    {"quad/128/r166", 128, k_modes<15, 13, 6, 6, true, true, 128, 3>, k_modes_batch<15, 13, 6, 6, true, true, 128, 3>},
-    {"quad/128/r128", 128, k_modes<15, 13, 6, 6, true, true, 128, 4>, k_modes_batch<15, 13, 6, 6, true, true, 128, 4>},
-    {"quad/256/r128", 256, k_modes<15, 13, 6, 6, true, true, 256, 2>, k_modes_batch<15, 13, 6, 6, true, true, 256, 2>},
+    {"quad/128/r166", 128, k_modes<kVKL, kVKU, 6, 6, true, true, 128, 3>, k_modes_batch<kVKL, kVKU, 6, 6, true, true, 128, 3>},
+    {"quad/128/r128", 128, k_modes<kVKL, kVKU, 6, 6, true, true, 128, 4>, k_modes_batch<kVKL, kVKU, 6, 6, true, true, 128, 4>},
+    {"quad/256/r128", 256, k_modes<kVKL, kVKU, 6, 6, true, true, 256, 2>, k_modes_batch<kVKL, kVKU, 6, 6, true, true, 256, 2>},
 };
 
 int resident(void (*kernel)(BatchTable<ModeArgs>, int *), int block) {

@@ -14,9 +14,9 @@ struct Variant {
   void (*kernel)(ModeArgs);
 };
 const Variant kVariants[] = {
-    {"split/64/r128", 64, k_modes_split<15, 13, 6, 6, 64, 8>},
-    {"split/128/r128", 128, k_modes_split<15, 13, 6, 6, 128, 4>},
-    {"split/64/r166", 64, k_modes_split<15, 13, 6, 6, 64, 6>},
+    {"split/64/r128", 64, k_modes_split<kVKL, kVKU, 6, 6, 64, 8>},
+    {"split/128/r128", 128, k_modes_split<kVKL, kVKU, 6, 6, 128, 4>},
+    {"split/64/r166", 64, k_modes_split<kVKL, kVKU, 6, 6, 64, 6>},
 };
 }  // namespace
 

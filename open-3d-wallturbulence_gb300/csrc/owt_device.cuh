@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "setup_host.h"  // kVKL, kVKU
+
 namespace owt {
 
 // Ring slot of history level 0 at step counter s (level l is (head + l) mod 3).
@@ -361,33 +363,33 @@ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const 
 // outside.  The first Masks::lo and the last Masks::hi columns keep the
 // boundary closures' own fill and are swept with the full band: the widths
 // are those beyond which the sweep found every column inside its type's masks
-// (eighth order: columns up to 38 from the bottom and 29 from the top lie
-// outside, sixth order 42 and 21, the omega_y-system 11 and 9), rounded up.
+// (v-system, both orders: columns up to 41 from the bottom and 30 from the
+// top lie outside; the omega_y-system 11 and 9), rounded up.
 // Register rings are padded to multiples of NT so that the unknown type
 // of every unrolled step is a compile-time constant (n is a multiple of NT).
 // Mask bit t set: L[c+t][c] may be nonzero (forward), U[c-t][c] (backward),
 // row interchange with offset t may occur (pivots).
 // ---------------------------------------------------------------------------
-// v-system (v, d1, d2, d3 per interior node): 26.25 entries per column
-// instead of 43 (the reference's eighth-order operators; the sixth-order
-// option has masks of its own, vmask6_* / VMasks6 below, checked at setup by
-// launch_check_pattern with type 2)
+// v-system (d3, d2, d1, v per interior node, types 0..3 in that order):
+// 21.5 entries per column instead of 46 (the reference's eighth-order
+// operators; the sixth-order option has masks of its own, vmask6_* / VMasks6
+// below, checked at setup by launch_check_pattern with type 2)
 __host__ __device__ constexpr unsigned long long vmask_l(int ty) {
-  return ty == 0 ? 0x3ffeull : ty == 1 ? 0x1ffeull : ty == 2 ? 0xffeull : 0x7feull;
+  return ty == 0 ? 0xcfeull : ty == 1 ? 0x6feull : ty == 2 ? 0x3feull : 0x19feull;
 }
 __host__ __device__ constexpr unsigned long long vmask_u(int ty) {
-  return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1fffeull : 0x3ffeull;
+  return ty == 0 ? 0x1ffeull : ty == 1 ? 0x7feull : ty == 2 ? 0x1feull : 0xffffeull;
 }
 // pivot offsets that occur in interior columns (bit t: offset t; 0 is free)
 __host__ __device__ constexpr unsigned long long vmask_p(int ty) {
-  return ty == 0 ? 0x5eull : ty == 1 ? 0x6eull : ty == 2 ? 0x36ull : 0x3aull;
+  return ty == 0 ? 0x44ull : ty == 1 ? 0x26ull : ty == 2 ? 0x12ull : 0xaull;
 }
 // omega_y-system (d1, d2 per node): 9 entries per column instead of 18, and
 // no row interchange in interior columns
 __host__ __device__ constexpr unsigned long long gmask_l(int ty) { return ty == 0 ? 0x3eull : 0x1eull; }
 __host__ __device__ constexpr unsigned long long gmask_u(int ty) { return ty == 0 ? 0x1eull : 0x3eull; }
 struct VMasks {
-  static constexpr int lo = 40, hi = 32;
+  static constexpr int lo = 44, hi = 32;
   __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask_p(ty); }
@@ -395,16 +397,16 @@ struct VMasks {
 // The sixth-order option (fd_order = 6) fills differently; its masks come
 // from the same derivation over the same sweep.
 __host__ __device__ constexpr unsigned long long vmask6_l(int ty) {
-  return ty == 0 ? 0xcffeull : ty == 1 ? 0x67feull : ty == 2 ? 0x33feull : 0x19feull;
+  return ty == 0 ? 0xcfeull : ty == 1 ? 0x67eull : ty == 2 ? 0x33eull : 0x19feull;
 }
 __host__ __device__ constexpr unsigned long long vmask6_u(int ty) {
-  return ty == 0 ? 0x3fffeull : ty == 3 ? 0x1ffeull : 0x3feull;
+  return ty == 0 ? 0x1feull : ty == 1 ? 0x7eull : ty == 2 ? 0x3eull : 0xffffeull;
 }
 __host__ __device__ constexpr unsigned long long vmask6_p(int ty) {
-  return ty == 0 ? 0x5eull : ty == 1 ? 0x1eull : ty == 2 ? 0x12ull : 0x8cull;
+  return ty == 0 ? 0x44ull : ty == 1 ? 0x4ull : ty == 2 ? 0x10ull : 0xcull;
 }
 struct VMasks6 {
-  static constexpr int lo = 44, hi = 24;
+  static constexpr int lo = 44, hi = 32;
   __host__ __device__ static constexpr unsigned long long l(int ty) { return vmask6_l(ty); }
   __host__ __device__ static constexpr unsigned long long u(int ty) { return vmask6_u(ty); }
   __host__ __device__ static constexpr unsigned long long p(int ty) { return vmask6_p(ty); }
@@ -515,17 +517,17 @@ template <class VM = VMasks, class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
-  band_solve_masked<15, 13, 4, 2, 16, 32, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
+  band_solve_masked<kVKL, kVKU, 4, 2, 16, 32, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 template <class VM = VMasks, class Rhs, class YStore>
 __device__ __forceinline__ void band_forward_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                       int n, int U, int u, Rhs rhs, YStore ystore) {
-  band_forward_masked<15, 13, 4, 2, 16, VM>(ab, piv, n, U, u, rhs, ystore);
+  band_forward_masked<kVKL, kVKU, 4, 2, 16, VM>(ab, piv, n, U, u, rhs, ystore);
 }
 template <class VM = VMasks, class YLoad, class Out>
 __device__ __forceinline__ void band_backward_v_sparse(const double *__restrict__ ab, int n, int U, int u,
                                                        YLoad yload, Out out) {
-  band_backward_masked<15, 13, 4, 2, 32, VM, double>(ab, n, U, u, yload, out);
+  band_backward_masked<kVKL, kVKU, 4, 2, 32, VM, double>(ab, n, U, u, yload, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,

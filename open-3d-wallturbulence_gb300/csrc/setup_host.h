@@ -40,7 +40,7 @@
 //
 // Equations are ordered by the midpoint of their column span (unknowns
 // interleaved by node); the resulting band widths are structural constants
-// (v-system kl = 15, ku = 13; omega_y-system kl = ku = 6) that the CUDA kernels
+// (v-system kl = 15, ku = 16 (kVKL, kVKU); omega_y-system kl = ku = 6) that the CUDA kernels
 // take as template parameters.  Band matrices are stored in LAPACK's
 // factorization layout (2kl+ku+1 rows, fill rows first) so that a partial-
 // pivoting band LU (the algorithm of LAPACK dgbtf2/dgbtrs) runs in place.
@@ -79,16 +79,23 @@ struct Stencils {
 constexpr int kRhsTable = 0, kRhsNone = -1, kRhsWallBottom = -2, kRhsWallTop = -3;
 
 // Column of unknown type t at node j in the v-system (types 0..3 = v, h d1,
-// h^2 d2, h^3 d3 at every node; type 4 = h^4 d4 only at nodes 0, 1, N-2, N-1).
+// h^2 d2, h^3 d3 at every node; type 4 = h^4 d4 only at nodes 0, 1, N-2,
+// N-1).  The four nodes at the walls hold their unknowns in type order; the
+// interior nodes in reverse (h^3 d3, h^2 d2, h d1, v): with the equations
+// sorted by the midpoint of their column spans, partial pivoting then fills
+// 78 entries of L and U per interior node instead of 105 (the union over the
+// mask derivation's sweep), for band widths 15 below and 16 above the
+// diagonal instead of 15 and 13.
+constexpr int kVKL = 15, kVKU = 16;
 __host__ __device__ inline int vcol(int t, int j, int N) {
-  return j < 2 ? 5 * j + t : j < N - 2 ? 10 + 4 * (j - 2) + t : 4 * N - 6 + 5 * (j - (N - 2)) + t;
+  return j < 2 ? 5 * j + t : j < N - 2 ? 10 + 4 * (j - 2) + (3 - t) : 4 * N - 6 + 5 * (j - (N - 2)) + t;
 }
 __host__ __device__ inline void vcol_split(int c, int N, int &t, int &j) {
   if (c < 10) {
     j = c / 5; t = c - 5 * j;
   } else if (c < 4 * N - 6) {
     const int q = c - 10;
-    j = 2 + (q >> 2); t = q & 3;
+    j = 2 + (q >> 2); t = 3 - (q & 3);
   } else {
     const int q = c - (4 * N - 6);
     j = N - 2 + q / 5; t = q - 5 * (q / 5);

@@ -228,7 +228,7 @@ static void factor_t(int kernel, double *ab, uint8_t *piv, int n, int U, const d
 void launch_band_factor(int kl, int ku, double *ab, uint8_t *piv, int n, int U, const double *t0,
                         const double *t1, const double *t2, const double *s1, const double *s2, double *rscale,
                         int *info, cudaStream_t st, int kernel) {
-  if (kl == 15 && ku == 13) factor_t<15, 13>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
+  if (kl == kVKL && ku == kVKU) factor_t<kVKL, kVKU>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
   else if (kl == 6 && ku == 6) factor_t<6, 6>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
   else if (kl == 2 && ku == 2) factor_t<2, 2>(kernel, ab, piv, n, U, t0, t1, t2, s1, s2, rscale, info, st);
 }
@@ -302,7 +302,7 @@ int band_factor_selftest(int kl, int ku, int n, int U, uint64_t seed, long long 
 }
 
 bool band_supported(int kl, int ku) {
-  return (kl == 15 && ku == 13) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
+  return (kl == kVKL && ku == kVKU) || (kl == 6 && ku == 6) || (kl == 2 && ku == 2);
 }
 
 // Mode-kernel variants live in modes_pair.cu and modes_quad.cu (separate
@@ -320,7 +320,7 @@ const char *modes_variant_name(int v) {
   return modes_split_name(v - modes_quad_count());
 }
 void launch_modes(const ModeArgs &a, int klv, int kuv, int klg, int kug, bool sparse, int variant, cudaStream_t st) {
-  if (!(klv == 15 && kuv == 13 && klg == 6 && kug == 6)) return;
+  if (!(klv == kVKL && kuv == kVKU && klg == 6 && kug == 6)) return;
   if (!sparse) { modes_dense_launch(a, st); return; }
   if (variant < modes_pair_count()) { modes_pair_launch(variant, a, st); return; }
   variant -= modes_pair_count();
@@ -370,9 +370,9 @@ __global__ void k_check_pattern(const double *__restrict__ ab, const uint8_t *__
 void launch_check_pattern(int which, const double *ab, const uint8_t *piv, int n, int U, int *bad,
                           cudaStream_t st) {
   if (which == 0)
-    k_check_pattern<15, 13, 4, 2, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+    k_check_pattern<kVKL, kVKU, 4, 2, VMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
   else if (which == 2)
-    k_check_pattern<15, 13, 4, 2, VMasks6><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
+    k_check_pattern<kVKL, kVKU, 4, 2, VMasks6><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
   else
     k_check_pattern<6, 6, 2, 0, GMasks><<<(U + 127) / 128, 128, 0, st>>>(ab, piv, n, U, bad);
 }

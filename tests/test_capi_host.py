@@ -70,6 +70,6 @@ def test_batch_seeded_and_selftest_entry_points_refuse_bad_arguments_without_a_g
     assert lib.owt_setup_report(None) == b""
     bad, t1, t2 = C.c_int64(0), C.c_float(0), C.c_float(0)
     # band widths the library does not use, and empty systems, are refused before any device work
-    assert lib.owt_band_factor_selftest(3, 3, 10, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
-    assert lib.owt_band_factor_selftest(15, 13, 0, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
+    assert lib.owt_band_factor_selftest(15, 13, 10, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
+    assert lib.owt_band_factor_selftest(15, 16, 0, 4, 1, C.byref(bad), C.byref(t1), C.byref(t2)) == L.OK + 1
     assert "bad arguments" in lib.owt_last_error(None).decode()

@@ -509,8 +509,8 @@ def test_reference_retau550_case_size_lamb_vector_and_steps(gpu_lib):
     m.close()
 
 
-@pytest.mark.parametrize("kl,ku,n,U", [(15, 13, 264, 600), (15, 13, 392, 1500), (6, 6, 196, 700), (2, 2, 97, 1),
-                                       (15, 13, 1028, 2048)])
+@pytest.mark.parametrize("kl,ku,n,U", [(15, 16, 264, 600), (15, 16, 392, 1500), (6, 6, 196, 700), (2, 2, 97, 1),
+                                       (15, 16, 1032, 2048)])
 def test_warp_band_factorization_is_bitwise_the_thread_one(gpu_lib, kl, ku, n, U):
     """The warp-per-system LU (channels with few modes) gives the same bits as
     the thread-per-system LU: factors, pivots and row scales."""
