@@ -123,12 +123,12 @@ def stage_work(p, precision="fp64"):
 
 
 # DRAM traffic per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-# of the 128x129x128 workload (profiles/k_xlamb_k_zback_channel180.md and
-# profiles/k_modes_channel180.md), scaled to
-# a launch at another size by the units the kernel processes (traffic grows in
-# proportion: y-z lines times kx modes for the transforms, modes times NY for the
-# mode kernel).
-NCU_TRAFFIC_128 = {"xlamb_fp64": 198.25e6, "modes": 1.355e9}
+# of the 128x129x128 workload (profiles/k_zback_k_xlamb_k_zfwd_fp64_channel180.md
+# and profiles/k_modes_split_k_mean_channel180.md), scaled to a launch at
+# another size by the units the kernel processes (traffic grows in proportion:
+# y-z lines times kx modes for the transforms, modes times NY for the mode
+# kernel).
+NCU_TRAFFIC_128 = {"xlamb_fp64": 198.33e6, "modes": 1.265e9}
 
 
 def scaled_traffic(kernel, p, precision):
