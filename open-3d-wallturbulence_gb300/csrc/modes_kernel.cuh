@@ -293,6 +293,7 @@ void modes_sixth_launch(const ModeArgs &a, cudaStream_t st);  // the sixth-order
 int modes_split_count();
 const char *modes_split_name(int v);
 void modes_split_launch(int v, const ModeArgs &a, cudaStream_t st);
+bool modes_split_is_quad(int v);
 int modes_quad_count();
 const char *modes_quad_name(int v);
 void modes_quad_launch(int v, const ModeArgs &a, cudaStream_t st);

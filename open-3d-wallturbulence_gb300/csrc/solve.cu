@@ -307,12 +307,16 @@ bool band_supported(int kl, int ku) {
 
 // Mode-kernel variants live in modes_pair.cu and modes_quad.cu (separate
 // translation units so they compile in parallel); this dispatches by index.
-// Variants: the pair mapping's, then the quad mapping's, then the split
-// mapping's (single-channel launches only; batches choose among the first
-// two families).
+// Variants: the pair mapping's, then the quad mapping's, then those for
+// single-channel launches only (modes_split.cu; batches choose among the
+// first two families).
 int modes_variant_count() { return modes_pair_count() + modes_quad_count() + modes_split_count(); }
 int modes_batch_variant_count() { return modes_pair_count() + modes_quad_count(); }
-bool modes_variant_is_quad(int v) { return v >= modes_pair_count() && v < modes_pair_count() + modes_quad_count(); }
+bool modes_variant_is_quad(int v) {
+  if (v < modes_pair_count()) return false;
+  v -= modes_pair_count();
+  return v < modes_quad_count() || modes_split_is_quad(v - modes_quad_count());
+}
 const char *modes_variant_name(int v) {
   if (v < modes_pair_count()) return modes_pair_name(v);
   v -= modes_pair_count();
