@@ -231,7 +231,7 @@ __device__ __forceinline__ void mode_body(const ModeArgs &a, const int tid, cons
     if (SPARSE) {
       if (active) band_forward_v_sparse<VM>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys);
       if (ROLE == 2) named_bar_sync(bar, 64);
-      if (active) band_backward_v_sparse<VM>(a.ab_v, a.n_v, a.U, u, yl, out);
+      if (active) band_backward_v_sparse<VM>(a.ab_v, a.n_v, a.U, u, yl, ys, out);
     } else {
       band_solve<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
     }

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "setup_host.h"  // kVKL, kVKU
 
 namespace owt {
@@ -502,6 +504,100 @@ __device__ __forceinline__ void band_backward_masked(const double *__restrict__ 
   }
 }
 
+// The backward sweep with two register rings: the full-band columns near the
+// walls need the whole upper band (KL + KU + 1 values in flight), the masked
+// interior only its deepest upper offset + 1 (WBI; 20 against 32 for the
+// v-system), and the smaller ring is what keeps the mode kernel within 128
+// registers without spilling.  Phase T: chunks of WBE columns from the top
+// while they are not all interior; phase I: chunks of WBI interior columns;
+// phase B: the rest in chunks of WBE.  Between phases the rows in flight move
+// ring to ring with compile-time slots; rows of the larger ring that the
+// smaller one cannot hold go back to the forward-swept values in memory
+// (ystore) with their pending updates, and are read again (yload) when they
+// enter the window: an interior column updates no row further than WBI - 1
+// below it.  Same operations in the same order as band_backward_masked.
+template <class Masks, int NT>
+__host__ __device__ constexpr int masks_u_reach() {
+  int r = 0;
+  for (int ty = 0; ty < NT; ++ty)
+    for (int t = 1; t < 64; ++t)
+      if ((Masks::u(ty) >> t) & 1ull) r = t > r ? t : r;
+  return r;
+}
+template <int KL, int KU, int NT, int OFF, int WBI, class Masks, class V, class YLoad, class YStore, class Out>
+__device__ __forceinline__ void band_backward_masked2(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
+                                                      YStore ystore, Out out) {
+  constexpr int KV = KL + KU;
+  constexpr int WBE = (KV + 1 + NT - 1) / NT * NT;
+  static_assert(WBI % NT == 0 && WBI < WBE, "ring sizes");
+  static_assert(masks_u_reach<Masks, NT>() < WBI, "interior ring shorter than the masks' upper reach");
+  const size_t sn = (size_t)n * U;
+  // column j at unrolled step s of a chunk that starts a multiple of NT below
+  // n - 1 (n is a multiple of NT): type (OFF - 1 - s) mod NT; ring of R slots
+  auto column = [&](auto ring, auto masked, int s, int j, auto &w) {
+    constexpr int R = decltype(ring)::value;
+    const double *col = ab + (size_t)j * U + u;
+    const V x = scal(w[s], col[(size_t)KV * sn]);
+    out(j, x);
+    if constexpr (decltype(masked)::value) {
+#pragma unroll
+      for (int t = 1; t < R; ++t)
+        if ((Masks::u((OFF - 1 - s % NT + 2 * NT) % NT) >> t) & 1ull)
+          fms(w[(s + t) % R], col[(size_t)(KV - t) * sn], x);
+    } else {
+      static_assert(R > KV, "a full-band column needs the full ring");
+#pragma unroll
+      for (int t = 1; t <= KV; ++t) fms(w[(s + t) % R], col[(size_t)(KV - t) * sn], x);
+    }
+    w[s] = (j - R >= 0) ? yload(j - R) : vzero<V>();
+  };
+  using E = std::integral_constant<int, WBE>;
+  using I = std::integral_constant<int, WBI>;
+  using Masked = std::true_type;
+  using Full = std::false_type;
+  auto interior = [&](int top, int len) { return top < n - Masks::hi && top - (len - 1) >= Masks::lo; };
+  int jj = 0;  // columns done, from the top
+  V we[WBE];
+#pragma unroll
+  for (int t = 0; t < WBE; ++t) we[t] = (n - 1 - t >= 0) ? yload(n - 1 - t) : vzero<V>();
+  // phase T: full-ring chunks until an interior-ring chunk would be all interior
+  for (; jj < n && !interior(n - 1 - jj, WBI); jj += WBE) {
+    if (interior(n - 1 - jj, WBE)) {
+#pragma unroll
+      for (int s = 0; s < WBE; ++s) column(E{}, Masked{}, s, n - 1 - (jj + s), we);
+    } else {
+#pragma unroll
+      for (int s = 0; s < WBE; ++s)
+        if (n - 1 - (jj + s) >= 0) column(E{}, Full{}, s, n - 1 - (jj + s), we);
+    }
+  }
+  if (jj >= n) return;
+  // to the interior ring: row n-1-jj-s in slot s; the deeper rows back to memory
+  V wi[WBI];
+#pragma unroll
+  for (int t = 0; t < WBI; ++t) wi[t] = we[t];
+#pragma unroll
+  for (int t = WBI; t < WBE; ++t)
+    if (n - 1 - jj - t >= 0) ystore(n - 1 - jj - t, we[t]);
+  // phase I
+  for (; jj < n && interior(n - 1 - jj, WBI); jj += WBI) {
+#pragma unroll
+    for (int s = 0; s < WBI; ++s) column(I{}, Masked{}, s, n - 1 - (jj + s), wi);
+  }
+  if (jj >= n) return;
+  // back to the full ring for the bottom columns
+#pragma unroll
+  for (int t = 0; t < WBI; ++t) we[t] = wi[t];
+#pragma unroll
+  for (int t = WBI; t < WBE; ++t) we[t] = (n - 1 - jj - t >= 0) ? yload(n - 1 - jj - t) : vzero<V>();
+  // phase B
+  for (; jj < n; jj += WBE) {
+#pragma unroll
+    for (int s = 0; s < WBE; ++s)
+      if (n - 1 - (jj + s) >= 0) column(E{}, Full{}, s, n - 1 - (jj + s), we);
+  }
+}
+
 template <int KL, int KU, int NT, int OFF, int W, int WB, class Masks, class Rhs, class YStore,
           class YLoad, class Out>
 __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
@@ -524,10 +620,10 @@ __device__ __forceinline__ void band_forward_v_sparse(const double *__restrict__
                                                       int n, int U, int u, Rhs rhs, YStore ystore) {
   band_forward_masked<kVKL, kVKU, 4, 2, 16, VM>(ab, piv, n, U, u, rhs, ystore);
 }
-template <class VM = VMasks, class YLoad, class Out>
+template <class VM = VMasks, class YLoad, class YStore, class Out>
 __device__ __forceinline__ void band_backward_v_sparse(const double *__restrict__ ab, int n, int U, int u,
-                                                       YLoad yload, Out out) {
-  band_backward_masked<kVKL, kVKU, 4, 2, 32, VM, double>(ab, n, U, u, yload, out);
+                                                       YLoad yload, YStore ystore, Out out) {
+  band_backward_masked2<kVKL, kVKU, 4, 2, 20, VM, double>(ab, n, U, u, yload, ystore, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
 __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
