@@ -107,8 +107,9 @@ def stage_work(p, precision="fp64"):
     NY, M, NXH, NZ2, NX2 = p.NY, p.NZ * p.NXH, p.NXH, p.NZ2, p.NX2
     S = 16.0 * NY * M  # bytes per spectral field (complex128)
     P = (16.0 if precision == "fp64" else 8.0) * NY * NZ2 * NXH  # one z-padded plane set
-    # banded systems: v-system 4NY+4 unknowns (kl 15, ku 13), omega_y-system 2NY (6, 6);
-    # per column and complex rhs: 2 * 2 * (2 kl + ku) flops (forward + backward)
+    # banded systems: v-system 4NY+4 unknowns (kl 15, ku 13: its band with the unknowns in
+    # node order, kept as the fixed count), omega_y-system 2NY (6, 6); per column and
+    # complex rhs: 2 * 2 * (2 kl + ku) flops (forward + backward)
     fl_modes = M * ((4 * NY + 4) * 4 * (2 * 15 + 13) + 2 * NY * 4 * (2 * 6 + 6) + 120 * NY)
     fl_fft = lambda n: 5.0 * n * math.log2(n)
     unique = NXH * (p.NZ // 2 + 1)
@@ -128,7 +129,7 @@ def stage_work(p, precision="fp64"):
 # another size by the units the kernel processes (traffic grows in proportion:
 # y-z lines times kx modes for the transforms, modes times NY for the mode
 # kernel).
-NCU_TRAFFIC_128 = {"xlamb_fp64": 198.33e6, "modes": 1.265e9}
+NCU_TRAFFIC_128 = {"xlamb_fp64": 198.33e6, "modes": 1.251e9}
 
 
 def scaled_traffic(kernel, p, precision):
