@@ -238,6 +238,9 @@ struct owt_handle {
     // eight, whose DY2 v re-derivations compete with the mode kernel)
     static constexpr int kChunks = 8, kDefaultChunks = 2;
     double2 *stage[12] = {}, *dstage[2] = {nullptr, nullptr};
+    // pinned host staging of the six friction values in and out, so that
+    // their copies are asynchronous like the uploads around them
+    double *fric_pin = nullptr;
     cudaEvent_t landed[kChunks] = {}, v_done[kChunks] = {}, q_done[kChunks] = {}, tx_done[kChunks] = {};
     cudaEvent_t up_done = nullptr, after_modes = nullptr, down_done = nullptr;
   } hs;

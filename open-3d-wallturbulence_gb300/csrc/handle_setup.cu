@@ -25,6 +25,7 @@ owt_handle::~owt_handle() {
     for (cudaEvent_t e : {hs.up_done, hs.after_modes, hs.down_done})
       if (e) cudaEventDestroy(e);
     for (cudaStream_t q : {hs.up, hs.tx, hs.aux, hs.down}) cudaStreamDestroy(q);
+    if (hs.fric_pin) cudaFreeHost(hs.fric_pin);
   }
   if (st2) cudaStreamDestroy(st2);
   if (st) cudaStreamDestroy(st);

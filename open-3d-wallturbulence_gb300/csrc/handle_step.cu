@@ -464,12 +464,26 @@ void owt_handle::host_step_prepare() {
   ck(cudaStreamCreateWithPriority(&hs.down, cudaStreamNonBlocking, hi), "stream");
   for (int i = 0; i < 12; ++i) hs.stage[i] = dalloc<double2>(fs, owned);
   for (int b = 0; b < 2; ++b) hs.dstage[b] = dalloc<double2>(fs, owned);
+  ck(cudaHostAlloc(reinterpret_cast<void **>(&hs.fric_pin), 12 * sizeof(double), cudaHostAllocDefault), "pinned");
   for (int j = 0; j < HostStep::kChunks; ++j)
     for (cudaEvent_t *e : {&hs.landed[j], &hs.v_done[j], &hs.q_done[j], &hs.tx_done[j]})
       ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
   for (cudaEvent_t *e : {&hs.up_done, &hs.after_modes, &hs.down_done})
     ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
   hs.ready = true;
+}
+
+// The device address of a host array the kernels can read directly (pinned
+// or registered memory, 16-byte aligned), or null.
+static const double2 *device_view(const double *p) {
+  if (reinterpret_cast<uintptr_t>(p) % 16 != 0) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<const double2 *>(at.devicePointer);
 }
 
 // Uploads, by chunks of Fourier modes: the modes with |kz| in a range are
@@ -481,7 +495,11 @@ void owt_handle::host_step_prepare() {
 // the chunk's modes is re-derived on a third stream, and the mode kernel
 // runs on the chunk's unique modes while the next chunks arrive.  One chunk
 // (everything) when the mode-kernel variant in use is not the quad mapping,
-// whose unique-mode ranges the chunks are.  Downloads: the new v and omega_y
+// whose unique-mode ranges the chunks are.  History fields in pinned memory
+// are uploaded by SM loads (launch_host_load), others by the copy engines:
+// at 384x257x384 copy-engine uploads of pinned memory ran at a tenth of the
+// host link's rate in every fourth or fifth call (about 230 instead of 80 ms
+// a call), SM loads at the full rate in every call.  Downloads: the new v and omega_y
 // are final after the mode kernel, so their transposes (high priority) and
 // copies run beside the transforms of the same step.
 void owt_handle::step_host(const double *const *hist, const double *means, const double *fric, double *v_out,
@@ -499,16 +517,18 @@ void owt_handle::step_host(const double *const *hist, const double *means, const
        "H2D");
   ck(cudaEventRecord(hs.up_done, hs.up), "means done");
   {
-    double fx[3], fz[3];
+    double *fx = hs.fric_pin, *fz = hs.fric_pin + 3;
     for (int l = 0; l < 3; ++l) {
       fx[slot(l)] = fric[l];
       fz[slot(l)] = fric[3 + l];
     }
-    ck(cudaMemcpyAsync(fx_ring, fx, sizeof(fx), cudaMemcpyHostToDevice, st), "H2D");
-    ck(cudaMemcpyAsync(fz_ring, fz, sizeof(fz), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(fx_ring, fx, 3 * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(fz_ring, fz, 3 * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
   }
   double2 *rings[4] = {v_ring, g_ring, hv_ring, hg_ring};
   const size_t row = (size_t)NXH * NY;  // complex values of one kz row, reference layout
+  const double2 *hdev[12];
+  for (int i = 0; i < 12; ++i) hdev[i] = device_view(hist[i]);
   // row blocks [k0, k1) of chunk j: |kz| in [a, b) for kz <= NZH, and the
   // negative partners NZ - |kz| for 1 <= |kz| < NZH
   auto blocks = [&](int j, int (&k0)[2], int (&k1)[2]) {
@@ -527,9 +547,15 @@ void owt_handle::step_host(const double *const *hist, const double *means, const
     blocks(j, k0, k1);
     for (int i = 0; i < 12; ++i)
       for (int q = 0; q < 2; ++q)
-        if (k1[q] > k0[q])
-          ck(cudaMemcpyAsync(hs.stage[i] + k0[q] * row, hist[i] + 2 * k0[q] * row, (k1[q] - k0[q]) * row * sizeof(double2),
-                             cudaMemcpyHostToDevice, hs.up), "H2D");
+        if (k1[q] > k0[q]) {
+          const size_t off = k0[q] * row, bytes = (k1[q] - k0[q]) * row * sizeof(double2);
+          if (hdev[i]) {
+            launch_host_load(hdev[i] + off, hs.stage[i] + off, bytes, hs.up);
+            ++launches;
+          } else {
+            ck(cudaMemcpyAsync(hs.stage[i] + off, hist[i] + 2 * off, bytes, cudaMemcpyHostToDevice, hs.up), "H2D");
+          }
+        }
     ck(cudaEventRecord(hs.landed[j], hs.up), "landed");
   }
   ck(cudaStreamWaitEvent(st, hs.up_done, 0), "means wait");
@@ -600,9 +626,9 @@ void owt_handle::step_host(const double *const *hist, const double *means, const
   ck(cudaEventRecord(hs.down_done, hs.down), "downloads done");
   ck(cudaStreamWaitEvent(st, hs.down_done, 0), "downloads wait");
   check_launch("host step");
-  double fx[3], fz[3];
-  ck(cudaMemcpyAsync(fx, fx_ring, sizeof(fx), cudaMemcpyDeviceToHost, st), "D2H");
-  ck(cudaMemcpyAsync(fz, fz_ring, sizeof(fz), cudaMemcpyDeviceToHost, st), "D2H");
+  double *fx = hs.fric_pin + 6, *fz = hs.fric_pin + 9;
+  ck(cudaMemcpyAsync(fx, fx_ring, 3 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+  ck(cudaMemcpyAsync(fz, fz_ring, 3 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
   sync_and_check();
   for (int l = 0; l < 3; ++l) {
     fric_out[l] = fx[slot(l)];

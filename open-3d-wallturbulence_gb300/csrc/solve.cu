@@ -870,6 +870,17 @@ void launch_transpose_ld(const double2 *in, double2 *out, int rows, int cols, in
   dim3 b(32, 8), g((cols + 31) / 32, (rows + 31) / 32);
   k_transpose_ld<<<g, b, 0, st>>>(in, out, rows, cols, ldo);
 }
+// Host -> device copy by the SMs: 16-byte loads of device-addressable host
+// memory (pinned, or any host memory on a system with coherent host access)
+// over the host link, grid-strided over one block per SM.
+__global__ void k_host_load(const float4 *__restrict__ src, float4 *__restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+void launch_host_load(const void *src, void *dst, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return;
+  k_host_load<<<152, 256, 0, st>>>(static_cast<const float4 *>(src), static_cast<float4 *>(dst), bytes / 16);
+}
 // Physical fields: [y][z][x] (device) <-> [z][x][y] (the reference's
 // Field<double> layout), a rows x cols transpose of doubles.
 __global__ void k_transpose_real(const double *__restrict__ in, double *__restrict__ out, int rows, int cols) {

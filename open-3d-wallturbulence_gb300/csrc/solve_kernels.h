@@ -176,6 +176,9 @@ void launch_transpose(const double2 *in, double2 *out, int rows, int cols, cudaS
 void launch_transpose_ld(const double2 *in, double2 *out, int rows, int cols, int ldo, cudaStream_t st);
 // the same for a rows x cols matrix of doubles
 void launch_transpose_real(const double *in, double *out, int rows, int cols, cudaStream_t st);
+// bytes (a multiple of 16) from device-addressable host memory, both
+// addresses 16-byte aligned, copied by SM loads
+void launch_host_load(const void *src, void *dst, size_t bytes, cudaStream_t st);
 void launch_stats(const double2 *u, const double2 *v, const double2 *w, int NY, int NZ, int NXH, double *out,
                   cudaStream_t st);
 

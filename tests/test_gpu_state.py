@@ -191,9 +191,11 @@ def test_host_state_step_equals_device_step(gpu_lib, precision, variant):
     overlapped with the device work) gives the bits of uploading the same
     state with the set-field calls and stepping, whatever the receiving
     handle's own ring position: the returned v, omega_y and friction, and the
-    handle's state afterwards, on two calls in a row.  With a quad-mapping
-    mode kernel the call pipelines the uploads with the mode kernel over
-    chunks of Fourier modes; the result is the same bits.  Both re-derive the
+    handle's state afterwards, on two calls in a row, the first from pageable
+    host memory (copy-engine uploads), the second from pinned memory (uploads
+    by SM loads).  With a quad-mapping mode kernel the call pipelines the
+    uploads with the mode kernel over chunks of Fourier modes; the result is
+    the same bits.  Both re-derive the
     DY2 v history of the uploaded v levels, which an uninterrupted run
     carries from its own solves, so against the uninterrupted step they
     agree to the one-step bound (1e-10)."""
@@ -220,13 +222,24 @@ def test_host_state_step_equals_device_step(gpu_lib, precision, variant):
     c.time_Integration(1)
     a.time_Integration(1)
     b = GpuSolver(p, precision=precision)
+    b.init_fields(*seeded_velocity(p, seed=9))
+    b.time_Integration(1)  # a different ring position than c's (and the autotuner's report)
     if variant == "quad":
         assert b.info("sparse_solve") == 1
-        b.force_modes_variant(b.info("modes_variants") - 1)  # the last variant maps threads by quads
-    b.init_fields(*seeded_velocity(p, seed=9))
-    b.time_Integration(1)  # a different ring position than c's
-    for rep in range(2):
-        v, g, f = b.time_Integration_host(hist, means, fric)
+        names = [t.split("=")[0] for t in b.tuning_report().split(" -> ")[0].split()]
+        assert len(names) == b.info("modes_variants")
+        b.force_modes_variant(names.index(next(n for n in names if n.startswith("quad/"))))
+    import torch
+
+    def pinned(x):
+        t = torch.empty(x.shape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)
+        t = t.reshape(x.shape)
+        t[...] = x
+        return t
+
+    # pageable history (copy-engine uploads), then pinned (uploads by SM loads)
+    for h_in in (hist, [pinned(x) for x in hist]):
+        v, g, f = b.time_Integration_host(h_in, means, fric)
         np.testing.assert_array_equal(v, c.get("vely"))
         np.testing.assert_array_equal(g, c.get("vory"))
         np.testing.assert_array_equal(f, c.friction())
