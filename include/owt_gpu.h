@@ -150,7 +150,10 @@ int owt_time_integration(owt_handle *h, int64_t nsteps);
  * re-derived while the other fields arrive, with a quad-mapping mode kernel
  * the copies are pipelined with it over chunks of Fourier modes
  * (OWT_OPT_HOST_CHUNKS), and v and omega_y travel back while the step's
- * transforms run.  Pinned host arrays give the full copy rate.
+ * transforms run.  History arrays in pinned (page-locked) host memory whose
+ * addresses are 16-byte aligned are read by the GPU's own loads at the full
+ * host-link rate; other arrays go through the copy engines (pageable memory
+ * at a fraction of that rate).
  * Synchronous: when it returns, the outputs are written. */
 int owt_time_integration_host(owt_handle *h, const double *const *hist, const double *means, const double *fric,
                               double *vely, double *vory, double *fric_out);
