@@ -111,7 +111,13 @@ void owt_handle::adjoint_step(const double2 *tp, double wgt) {
     ma.fxb[l] = adj.fric[0][l]; ma.fzb[l] = adj.fric[1][l];
   }
   ma.scratch = adj.mscr;
-  launch_adj_mean(ma, st);
+  // the mean mode's adjoint (one block) on the high-priority second stream,
+  // beside the mode kernel's: they share only read-only inputs (the adjoint
+  // fields of the Lamb vector) and write disjoint buffers
+  ck(cudaEventRecord(ev_fork, st), "fork");
+  ck(cudaStreamWaitEvent(st2, ev_fork, 0), "fork wait");
+  launch_adj_mean(ma, st2);
+  ck(cudaEventRecord(ev_join, st2), "join");
 
   AdjModeArgs mo{};
   mo.NY = NY; mo.NZ = NZ; mo.NXH = NXH; mo.NZH = NZH; mo.M = M; mo.U = Uq;
@@ -129,6 +135,7 @@ void owt_handle::adjoint_step(const double2 *tp, double wgt) {
   mo.xv0 = adj.xs[0]; mo.xv1 = adj.xs[1]; mo.xv2 = adj.xs[2]; mo.xg0 = adj.xs[3]; mo.xg1 = adj.xs[4];
   mo.sgb = adj.xs[5]; mo.svb = adj.xs[6];
   launch_adj_modes(mo, st);
+  ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launches += 6;
   check_launch("adjoint step");
   // the buffers now hold the adjoints of the levels the step read, level l

@@ -11,7 +11,10 @@ that a profiler restricted to that range sees exactly those launches:
 Stages: modes, mean, lamb, nonlinear, zback, xlamb, zfwd, mean_lamb (the
 stage numbers of owt_enqueue_stage).  Sizes default to the workload's; --nx,
 --ny, --nz override them (a smaller NY keeps the device memory of a capture
-to a few GB).
+to a few GB).  --adjoint N,INTERVAL profiles one wall-drag gradient instead
+(owt_drag_forward over N steps with device images every INTERVAL steps, then
+owt_drag_backward, with seeded wall blowing/suction), after one unprofiled
+evaluation.
 """
 import argparse
 import dataclasses
@@ -29,6 +32,7 @@ def main(argv=None):
     ap.add_argument("--nz", type=int)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--stages", default="modes")
+    ap.add_argument("--adjoint", help="N,INTERVAL: one wall-drag gradient evaluation")
     args = ap.parse_args(argv)
     import torch
     from owt import params
@@ -40,6 +44,25 @@ def main(argv=None):
     stages = [STAGES[s] for s in args.stages.split(",") if s]
     s = GpuSolver(p, precision=args.precision)
     s.init_seeded(0, 0.1)
+    if args.adjoint:
+        from owt.adjoint import seeded_wall_field
+        n, interval = (int(x) for x in args.adjoint.split(","))
+        s.use_graph(True)
+        s.keep_state()
+        s.set_wall_velocity(seeded_wall_field(p, 1), seeded_wall_field(p, 2))
+        for rep in range(2):
+            s.restore_state()
+            s.synchronize()
+            if rep:
+                torch.cuda.nvtx.range_push("prof")
+            s.drag_forward(n, interval)
+            s.drag_backward()
+            s.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print("profile case %dx%dx%d adjoint %s; device memory %.2f GB"
+              % (p.NX, p.NY, p.NZ, args.adjoint, s.info("device_bytes") / 1e9))
+        s.close()
+        return
     s.time_Integration(2)
     s.synchronize()
     torch.cuda.nvtx.range_push("prof")
