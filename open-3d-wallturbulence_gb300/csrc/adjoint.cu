@@ -24,7 +24,8 @@
 //               the augmented v- and omega_y-systems on the forward factors,
 //               and the source assembly^T into the three history levels.  The
 //               transposed v solve also yields d objective / d v_w from the
-//               two wall rows.
+//               two wall rows; it skips the entries outside the interior
+//               fill masks where the forward's masked solves apply.
 #include <cuda_runtime.h>
 
 #include "adjoint_kernels.h"
@@ -332,7 +333,9 @@ void launch_adj_mean(const AdjMeanArgs &a, cudaStream_t st) { k_adj_mean<<<1, 32
 // ---------------------------------------------------------------------------
 // Mode kernel adjoint, one thread per real component of a mode.
 // ---------------------------------------------------------------------------
-template <int KLV, int KUV, int KLG, int KUG>
+// VMODE: the v-system's transposed solve over the full band (0) or inside
+// the interior masks the setup check admitted (1: VMasks, 2: VMasks6).
+template <int KLV, int KUV, int KLG, int KUG, int VMODE>
 __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int m = tid >> 1, comp = tid & 1;
@@ -423,7 +426,12 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
         D(a.grad)[2 * ((size_t)M + m) + comp] += r;
       }
     };
-    band_solve_t<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    if constexpr (VMODE == 1)
+      band_solve_t_masked<KLV, KUV, 4, 2, VMasks>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    else if constexpr (VMODE == 2)
+      band_solve_t_masked<KLV, KUV, 4, 2, VMasks6>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
+    else
+      band_solve_t<KLV, KUV>(a.ab_v, a.piv_v, a.n_v, a.U, u, rhs, ys, yl, out);
     // source_v = sum beta Hv_l - k^2/dt sum alpha v_l + sum alpha q_l / dt on
     // nodes 2..NY-3; the tables reference no other node, so svb is zero there
     for (int j = 0; j < NY; ++j) {
@@ -456,9 +464,11 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
   }
 }
 
-void launch_adj_modes(const AdjModeArgs &a, cudaStream_t st) {
-  const int threads = 2 * a.M;
-  k_adj_modes<kVKL, kVKU, 6, 6><<<(threads + 127) / 128, 128, 0, st>>>(a);
+void launch_adj_modes(const AdjModeArgs &a, int vmode, cudaStream_t st) {
+  const int threads = 2 * a.M, grid = (threads + 127) / 128;
+  if (vmode == 1) k_adj_modes<kVKL, kVKU, 6, 6, 1><<<grid, 128, 0, st>>>(a);
+  else if (vmode == 2) k_adj_modes<kVKL, kVKU, 6, 6, 2><<<grid, 128, 0, st>>>(a);
+  else k_adj_modes<kVKL, kVKU, 6, 6, 0><<<grid, 128, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------

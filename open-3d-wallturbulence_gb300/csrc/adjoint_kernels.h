@@ -75,7 +75,9 @@ void launch_adj_nl(const AdjNLArgs &a, cudaStream_t st);
 cudaError_t adj_lamb_prepare(const XformDims &d);
 void launch_adj_lamb(const AdjXformArgs &a, cudaStream_t st);  // three launches
 void launch_adj_mean(const AdjMeanArgs &a, cudaStream_t st);
-void launch_adj_modes(const AdjModeArgs &a, cudaStream_t st);
+// vmode: 0 full band, 1 / 2 the v-system's transposed solve inside the
+// eighth- / sixth-order interior masks (only where the setup check passed)
+void launch_adj_modes(const AdjModeArgs &a, int vmode, cudaStream_t st);
 void launch_objective_add(const double *fx_ring, const long long *step, double weight, double *acc,
                           cudaStream_t st);
 size_t adj_zbuf_values(const XformDims &d);

@@ -134,7 +134,7 @@ void owt_handle::adjoint_step(const double2 *tp, double wgt) {
   mo.grad = adj.grad; mo.yv = adj.yv; mo.yg = adj.yg;
   mo.xv0 = adj.xs[0]; mo.xv1 = adj.xs[1]; mo.xv2 = adj.xs[2]; mo.xg0 = adj.xs[3]; mo.xg1 = adj.xs[4];
   mo.sgb = adj.xs[5]; mo.svb = adj.xs[6];
-  launch_adj_modes(mo, st);
+  launch_adj_modes(mo, force_dense ? 0 : sparse_v ? 1 : sparse_v6 ? 2 : 0, st);
   ck(cudaStreamWaitEvent(st, ev_join, 0), "join wait");
   launches += 6;
   check_launch("adjoint step");

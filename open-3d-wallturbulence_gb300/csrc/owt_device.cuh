@@ -706,4 +706,94 @@ __device__ __forceinline__ void band_solve_t(const double *__restrict__ ab, cons
   }
 }
 
+
+// The transposed solve with the interior columns of the factors restricted
+// to the fill and interchange masks of their type (Masks, column type
+// (c + OFF) mod NT), as band_solve_masked does for the solve itself: a ring
+// chunk whose columns all lie between the full-band edges (Masks::lo,
+// Masks::hi) skips the entries outside its columns' masks, which are exact
+// zeros in every factorization the setup check admits, so the result is
+// bitwise that of band_solve_t.  Needs n a multiple of NT (the column types
+// of the backward pass are then compile-time constants).
+template <int KL, int KU, int NT, int OFF, class Masks, class Rhs, class YStore, class YLoad, class Out>
+__device__ __forceinline__ void band_solve_t_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+                                                    int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
+                                                    Out out) {
+  using V = decltype(rhs(0));
+  constexpr int KV = KL + KU;
+  const size_t sn = (size_t)n * U;
+  {
+    // U^T y = b: column j's entries U(j - t, j), t in its type's upper mask
+    constexpr int W = KV + 1;
+    static_assert(W % NT == 0, "ring size");
+    V w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = vzero<V>();
+    for (int j0 = 0; j0 < n; j0 += W) {
+      const bool sparse = (j0 >= Masks::lo) && (j0 + W - 1 < n - Masks::hi);
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int j = j0 + s;
+        if (j < n) {
+          const double *col = ab + (size_t)j * U + u;
+          V acc = rhs(j);
+          if (sparse) {
+#pragma unroll
+            for (int t = 1; t <= KV; ++t)
+              if ((Masks::u((s + OFF) % NT) >> t) & 1ull) fms(acc, col[(size_t)(KV - t) * sn], w[(s - t + W) % W]);
+          } else {
+#pragma unroll
+            for (int t = 1; t <= KV; ++t) fms(acc, col[(size_t)(KV - t) * sn], w[(s - t + W) % W]);
+          }
+          acc = scal(acc, col[(size_t)KV * sn]);
+          w[s] = acc;
+          ystore(j, acc);
+        }
+      }
+    }
+  }
+  {
+    // L^T and the interchanges, j = n-1 .. 0; with n and jj multiples of NT
+    // the type of column j = n-1 - (jj + s) is (OFF - 1 - s) mod NT
+    constexpr int W = KL + 1;
+    static_assert(W % NT == 0, "ring size");
+    V w[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) w[t] = vzero<V>();
+    for (int jj = 0; jj < n + KL; jj += W) {
+      const bool sparse = (n - 1 - jj - (W - 1) >= Masks::lo) && (n - 1 - jj < n - Masks::hi);
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int ty = (((OFF - 1 - s) % NT) + NT) % NT;
+        const int j = n - 1 - (jj + s);
+        if (j >= 0) {
+          const double *col = ab + (size_t)j * U + u;
+          V acc = yload(j);
+          if (sparse) {
+#pragma unroll
+            for (int i = 1; i <= KL; ++i)
+              if ((Masks::l(ty) >> i) & 1ull) fms(acc, col[(size_t)(KV + i) * sn], w[(s - i + W) % W]);
+          } else {
+#pragma unroll
+            for (int i = 1; i <= KL; ++i) fms(acc, col[(size_t)(KV + i) * sn], w[(s - i + W) % W]);
+          }
+          w[s] = acc;
+          const int off = piv[(size_t)j * U + u];
+#pragma unroll
+          for (int i = 1; i <= KL; ++i) {
+            if ((!sparse || ((Masks::p(ty) >> i) & 1ull)) && off == i) {
+              const V tmp = w[s];
+              w[s] = w[(s - i + W) % W];
+              w[(s - i + W) % W] = tmp;
+            }
+          }
+        } else {
+          w[s] = vzero<V>();
+        }
+        const int c = j + KL;
+        if (c >= 0 && c < n) out(c, w[(s + 1) % W]);
+      }
+    }
+  }
+}
 }  // namespace owt
