@@ -331,13 +331,20 @@ __global__ void k_adj_mean(AdjMeanArgs a) {
 void launch_adj_mean(const AdjMeanArgs &a, cudaStream_t st) { k_adj_mean<<<1, 32, 0, st>>>(a); }
 
 // ---------------------------------------------------------------------------
-// Mode kernel adjoint, one thread per real component of a mode.
+// Mode kernel adjoint, two threads per real component of a mode (one per system).
 // ---------------------------------------------------------------------------
 // VMODE: the v-system's transposed solve over the full band (0) or inside
 // the interior masks the setup check admitted (1: VMasks, 2: VMasks6).
+// Blocks of two warps serve 16 modes (both real components): warp 0 the
+// v-system's part (its inputs from solve_horizontal^T, the transposed v
+// solve, the v, DY2 v and Hv histories), warp 1 the omega_y-system's (its
+// inputs, the transposed omega_y solve, the g and Hg histories).  The two
+// parts read and write disjoint data, so they need no synchronisation, and
+// each value comes from the same operations as in one thread doing both.
 template <int KLV, int KUV, int KLG, int KUG, int VMODE>
-__global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(64) k_adj_modes(AdjModeArgs a) {
+  const int role = threadIdx.x >> 5;  // 0: v-system, 1: omega_y-system
+  const int tid = blockIdx.x * 32 + (threadIdx.x & 31);
   const int m = tid >> 1, comp = tid & 1;
   if (m >= a.M) return;
   const int M = a.M, NY = a.NY;
@@ -364,42 +371,53 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
 
   // 1. solve_horizontal^T and the adjoints of the solves' outputs per node:
   //    v, D1 v (through DY1 v = c11 d1, DY2 v = c21 d1 + c22 d2), g, D1 g
+  //    (each warp the part its system reads)
   for (int j = 0; j < NY; ++j) {
     const bool in = j != 0 && j != NY - 1;
     const size_t at = (size_t)j * M + m;
-    double2 vt = a.v[0][at], qt = a.q[0][at], gt = a.g[0][at];
-    const double2 vf = a.vb[at], gf = a.gb[at];
-    vt.x += vf.x; vt.y += vf.y;
-    gt.x += gf.x; gt.y += gf.y;
-    double2 dv = make_double2(0.0, 0.0), dg = make_double2(0.0, 0.0);
-    if (horiz) {
-      const double2 ub = a.ub[at], wb = a.wb[at], oxb = a.oxb[at], ozb = a.ozb[at];
-      // adjoints of u = i ax DY1v - i az g, w = i ax g + i az DY1v,
-      // om_x = i/k2 (kx DY1g + kz DY2v) - i kz v, om_z = i/k2 (kz DY1g - kx DY2v) + i kx v
-      dv = make_double2(ax * ub.y + az * wb.y, -ax * ub.x - az * wb.x);
-      gt.x += -az * ub.y + ax * wb.y;
-      gt.y += az * ub.x - ax * wb.x;
-      dg = make_double2(ax * oxb.y + az * ozb.y, -ax * oxb.x - az * ozb.x);
-      qt.x += az * oxb.y - ax * ozb.y;
-      qt.y += -az * oxb.x + ax * ozb.x;
-      vt.x += -kz * oxb.y + kx * ozb.y;
-      vt.y += kz * oxb.x - kx * ozb.x;
-    }
     const double c11 = a.c11[j], c21 = a.c21[j], c22 = a.c22[j];
-    const double v_ = cmp(vt), q_ = cmp(qt), g_ = cmp(gt), dv_ = cmp(dv), dg_ = cmp(dg);
     const size_t e = E(j);
-    D(a.xv0)[e] = v_;
-    D(a.xv1)[e] = a.inv_h * (c11 * dv_ + c21 * q_);
-    D(a.xv2)[e] = a.inv_h2 * c22 * q_;
-    D(a.xg0)[e] = a.inv_h * (c11 * dg_ + (in ? nu * c21 * icg * g_ : 0.0));
-    D(a.xg1)[e] = in ? a.inv_h2 * nu * c22 * icg * g_ : 0.0;
-    D(a.sgb)[e] = in ? icg * g_ : 0.0;
+    if (role == 0) {
+      double2 vt = a.v[0][at], qt = a.q[0][at];
+      const double2 vf = a.vb[at];
+      vt.x += vf.x; vt.y += vf.y;
+      double2 dv = make_double2(0.0, 0.0);
+      if (horiz) {
+        const double2 ub = a.ub[at], wb = a.wb[at], oxb = a.oxb[at], ozb = a.ozb[at];
+        // adjoints of u = i ax DY1v - i az g, w = i ax g + i az DY1v,
+        // om_x = i/k2 (kx DY1g + kz DY2v) - i kz v, om_z = i/k2 (kz DY1g - kx DY2v) + i kx v
+        dv = make_double2(ax * ub.y + az * wb.y, -ax * ub.x - az * wb.x);
+        qt.x += az * oxb.y - ax * ozb.y;
+        qt.y += -az * oxb.x + ax * ozb.x;
+        vt.x += -kz * oxb.y + kx * ozb.y;
+        vt.y += kz * oxb.x - kx * ozb.x;
+      }
+      const double v_ = cmp(vt), q_ = cmp(qt), dv_ = cmp(dv);
+      D(a.xv0)[e] = v_;
+      D(a.xv1)[e] = a.inv_h * (c11 * dv_ + c21 * q_);
+      D(a.xv2)[e] = a.inv_h2 * c22 * q_;
+    } else {
+      double2 gt = a.g[0][at];
+      const double2 gf = a.gb[at];
+      gt.x += gf.x; gt.y += gf.y;
+      double2 dg = make_double2(0.0, 0.0);
+      if (horiz) {
+        const double2 ub = a.ub[at], wb = a.wb[at], oxb = a.oxb[at], ozb = a.ozb[at];
+        gt.x += -az * ub.y + ax * wb.y;
+        gt.y += az * ub.x - ax * wb.x;
+        dg = make_double2(ax * oxb.y + az * ozb.y, -ax * oxb.x - az * ozb.x);
+      }
+      const double g_ = cmp(gt), dg_ = cmp(dg);
+      D(a.xg0)[e] = a.inv_h * (c11 * dg_ + (in ? nu * c21 * icg * g_ : 0.0));
+      D(a.xg1)[e] = in ? a.inv_h2 * nu * c22 * icg * g_ : 0.0;
+      D(a.sgb)[e] = in ? icg * g_ : 0.0;
+    }
   }
 
   // 2. v-system^T: the source adjoint is scattered through the rows' rhs
   //    tables, then feeds Hv, v, DY2 v of the three levels; the two wall
   //    rows give the wall-velocity gradient
-  {
+  if (role == 0) {
     for (int j = 0; j < NY; ++j) D(a.svb)[E(j)] = 0.0;
     auto rhs = [&](int c) -> double {
       int t, jn;
@@ -443,7 +461,7 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
   }
 
   // 3. omega_y-system^T: source adjoint scattered through the B rows
-  {
+  else {
     auto rhs = [&](int c) -> double { return (c & 1) ? D(a.xg1)[E(c >> 1)] : D(a.xg0)[E(c >> 1)]; };
     auto ys = [&](int p, double y) { D(a.yg)[E(p)] = y; };
     auto yl = [&](int p) -> double { return D(a.yg)[E(p)]; };
@@ -465,10 +483,10 @@ __global__ void __launch_bounds__(128) k_adj_modes(AdjModeArgs a) {
 }
 
 void launch_adj_modes(const AdjModeArgs &a, int vmode, cudaStream_t st) {
-  const int threads = 2 * a.M, grid = (threads + 127) / 128;
-  if (vmode == 1) k_adj_modes<kVKL, kVKU, 6, 6, 1><<<grid, 128, 0, st>>>(a);
-  else if (vmode == 2) k_adj_modes<kVKL, kVKU, 6, 6, 2><<<grid, 128, 0, st>>>(a);
-  else k_adj_modes<kVKL, kVKU, 6, 6, 0><<<grid, 128, 0, st>>>(a);
+  const int grid = (2 * a.M + 31) / 32;  // 16 modes (32 real components) a block of two warps
+  if (vmode == 1) k_adj_modes<kVKL, kVKU, 6, 6, 1><<<grid, 64, 0, st>>>(a);
+  else if (vmode == 2) k_adj_modes<kVKL, kVKU, 6, 6, 2><<<grid, 64, 0, st>>>(a);
+  else k_adj_modes<kVKL, kVKU, 6, 6, 0><<<grid, 64, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------
