@@ -233,9 +233,9 @@ struct owt_handle {
     // and copies (high priority)
     cudaStream_t up = nullptr, tx = nullptr, aux = nullptr, down = nullptr;
     // chunks of Fourier modes the uploads and the mode kernel pipeline over:
-    // at most kChunks, kDefaultChunks unless set (measured at 384x257x384:
-    // 88.5 ms a call with one chunk, 82.7 with two, 85.8 with four, 110 with
-    // eight, whose DY2 v re-derivations compete with the mode kernel)
+    // at most kChunks, kDefaultChunks unless set (two measured fastest at
+    // 384x257x384, 6% ahead of one and of four; with eight the DY2 v
+    // re-derivations compete with the mode kernel, 25% slower)
     static constexpr int kChunks = 8, kDefaultChunks = 2;
     double2 *stage[12] = {}, *dstage[2] = {nullptr, nullptr};
     // pinned host staging of the six friction values in and out, so that
