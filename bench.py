@@ -351,6 +351,16 @@ def run_ours(args, rank, world, local_rank):
     roof["traffic_source"] = "ncu at 128x129x128, scaled by units processed (profiles/)"
     roof["peak_source"] = ("cuBLAS DGEMM (torch.matmul float64, 4096^3) measured in this run"
                            if roof["bound"] == "fp64" else f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})")
+    if roof["bound"] == "fp64":
+        # second denominator: the FP64 issue rate, two DFMA (4 flops) per clock per
+        # SM (ncu's sm__sass_thread_inst_executed_op_dfma_pred_on peak) at the SM
+        # clock sampled during the timed steps; `frac` stays against the DGEMM
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+        issue_peak = 4.0 * sms * mhz * 1e6 / 1e12
+        roof["peak_fp64_issue"] = {"value": round(issue_peak, 4), "unit": "TFLOP/s",
+                                   "frac": round(roof["achieved"] / issue_peak, 4),
+                                   "source": "2 DFMA per clock per SM x %d SMs x %.0f MHz" % (sms, mhz)}
     roof["stage_ms"] = {k: round(v, 4) for k, v in stage_ms.items()}
     roof["stage_hbm_gbs"] = {k: round(work[k]["bytes"] / (stage_ms[k] * 1e-3) / 1e9, 1) for k in stage_ms}
     roof["stage_fp64_tflops"] = {k: round(work[k]["flops"] / (stage_ms[k] * 1e-3) / 1e12, 3) for k in stage_ms}
