@@ -270,13 +270,13 @@ __device__ __forceinline__ cpx<T> hermitian_pair(const cpx<T> *A, const cpx<T> *
 
 // Value helpers so the band solves run on one real component (double) or a
 // complex value (double2) per thread.
-__device__ __forceinline__ void fms(double &w, double l, double y) { w -= l * y; }
-__device__ __forceinline__ void fms(double2 &w, double l, double2 y) { w.x -= l * y.x; w.y -= l * y.y; }
-__device__ __forceinline__ double scal(double w, double r) { return w * r; }
-__device__ __forceinline__ double2 scal(double2 w, double r) { return make_double2(w.x * r, w.y * r); }
-template <class V> __device__ __forceinline__ V vzero();
-template <> __device__ __forceinline__ double vzero<double>() { return 0.0; }
-template <> __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
+__host__ __device__ __forceinline__ void fms(double &w, double l, double y) { w -= l * y; }
+__host__ __device__ __forceinline__ void fms(double2 &w, double l, double2 y) { w.x -= l * y.x; w.y -= l * y.y; }
+__host__ __device__ __forceinline__ double scal(double w, double r) { return w * r; }
+__host__ __device__ __forceinline__ double2 scal(double2 w, double r) { return make_double2(w.x * r, w.y * r); }
+template <class V> __host__ __device__ __forceinline__ V vzero();
+template <> __host__ __device__ __forceinline__ double vzero<double>() { return 0.0; }
+template <> __host__ __device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
 
 // ---------------------------------------------------------------------------
 // Banded LU solve, the algorithm of LAPACK dgbtrs ('N') on factors produced by
@@ -297,7 +297,7 @@ template <> __device__ __forceinline__ double2 vzero<double2>() { return make_do
 //   out(c, x)   : solution entry for column c, produced for c = n-1 .. 0
 // ---------------------------------------------------------------------------
 template <int KL, int KU, class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
+__host__ __device__ __forceinline__ void band_solve(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
                                            int U, int u, Rhs rhs, YStore ystore, YLoad yload, Out out) {
   using V = decltype(rhs(0));
   constexpr int KV = KL + KU;
@@ -424,7 +424,7 @@ struct GMasks {
 // band_solve_masked, which exchange the forward-swept values only through
 // ystore / yload; a caller may run other work between them.
 template <int KL, int KU, int NT, int OFF, int W, class Masks, class Rhs, class YStore>
-__device__ __forceinline__ void band_forward_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_forward_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore) {
   static_assert(W >= KL + 1 && W % NT == 0, "ring size");
   using V = decltype(rhs(0));
@@ -468,7 +468,7 @@ __device__ __forceinline__ void band_forward_masked(const double *__restrict__ a
   }
 }
 template <int KL, int KU, int NT, int OFF, int WB, class Masks, class V, class YLoad, class Out>
-__device__ __forceinline__ void band_backward_masked(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
+__host__ __device__ __forceinline__ void band_backward_masked(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
                                                      Out out) {
   static_assert(WB >= KL + KU + 1 && WB % NT == 0, "ring size");
   constexpr int KV = KL + KU;
@@ -525,7 +525,7 @@ __host__ __device__ constexpr int masks_u_reach() {
   return r;
 }
 template <int KL, int KU, int NT, int OFF, int WBI, class Masks, class V, class YLoad, class YStore, class Out>
-__device__ __forceinline__ void band_backward_masked2(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
+__host__ __device__ __forceinline__ void band_backward_masked2(const double *__restrict__ ab, int n, int U, int u, YLoad yload,
                                                       YStore ystore, Out out) {
   constexpr int KV = KL + KU;
   constexpr int WBE = (KV + 1 + NT - 1) / NT * NT;
@@ -600,7 +600,7 @@ __device__ __forceinline__ void band_backward_masked2(const double *__restrict__
 
 template <int KL, int KU, int NT, int OFF, int W, int WB, class Masks, class Rhs, class YStore,
           class YLoad, class Out>
-__device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                   int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                   Out out) {
   using V = decltype(rhs(0));
@@ -610,23 +610,23 @@ __device__ __forceinline__ void band_solve_masked(const double *__restrict__ ab,
 
 // VM: VMasks (the reference's eighth-order operators) or VMasks6
 template <class VM = VMasks, class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_solve_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
   band_solve_masked<kVKL, kVKU, 4, 2, 16, 32, VM>(ab, piv, n, U, u, rhs, ystore, yload, out);
 }
 template <class VM = VMasks, class Rhs, class YStore>
-__device__ __forceinline__ void band_forward_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_forward_v_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                       int n, int U, int u, Rhs rhs, YStore ystore) {
   band_forward_masked<kVKL, kVKU, 4, 2, 16, VM>(ab, piv, n, U, u, rhs, ystore);
 }
 template <class VM = VMasks, class YLoad, class YStore, class Out>
-__device__ __forceinline__ void band_backward_v_sparse(const double *__restrict__ ab, int n, int U, int u,
+__host__ __device__ __forceinline__ void band_backward_v_sparse(const double *__restrict__ ab, int n, int U, int u,
                                                        YLoad yload, YStore ystore, Out out) {
   band_backward_masked2<kVKL, kVKU, 4, 2, 20, VM, double>(ab, n, U, u, yload, ystore, out);
 }
 template <class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
   band_solve_masked<6, 6, 2, 0, 8, 14, GMasks>(ab, piv, n, U, u, rhs, ystore, yload, out);
@@ -643,7 +643,7 @@ __device__ __forceinline__ void band_solve_g_sparse(const double *__restrict__ a
 //   out(c, x)   : solution entry c, produced for c = n-1 .. 0
 // ---------------------------------------------------------------------------
 template <int KL, int KU, class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve_t(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
+__host__ __device__ __forceinline__ void band_solve_t(const double *__restrict__ ab, const uint8_t *__restrict__ piv, int n,
                                              int U, int u, Rhs rhs, YStore ystore, YLoad yload, Out out) {
   using V = decltype(rhs(0));
   constexpr int KV = KL + KU;
@@ -716,7 +716,7 @@ __device__ __forceinline__ void band_solve_t(const double *__restrict__ ab, cons
 // bitwise that of band_solve_t.  Needs n a multiple of NT (the column types
 // of the backward pass are then compile-time constants).
 template <int KL, int KU, int NT, int OFF, class Masks, class Rhs, class YStore, class YLoad, class Out>
-__device__ __forceinline__ void band_solve_t_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
+__host__ __device__ __forceinline__ void band_solve_t_masked(const double *__restrict__ ab, const uint8_t *__restrict__ piv,
                                                     int n, int U, int u, Rhs rhs, YStore ystore, YLoad yload,
                                                     Out out) {
   using V = decltype(rhs(0));
